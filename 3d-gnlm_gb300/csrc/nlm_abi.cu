@@ -1,0 +1,390 @@
+// C ABI of libgnlm.so (declared in include/nlm.h): argument checks, status codes,
+// the per-thread error message, workspace management and the host-buffer path.
+#include <cudaTypedefs.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "../../include/nlm.h"
+#include "nlm_internal.h"
+
+namespace gnlm {
+
+// One error word per device; kernels OR DEVERR_* bits into it when a bounded
+// wait gives up (see nlm_device_status).
+__device__ unsigned int g_device_error_word;
+
+namespace {
+
+thread_local char t_last_error[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_last_error, sizeof(t_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorNotSupported)
+        return fail(NLM_ERR_UNSUPPORTED, "%s: combination not compiled in", what);
+    return fail(NLM_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+std::mutex g_mutex;
+std::map<int, unsigned int*> g_errword;                    // device -> error word address
+std::map<std::pair<int, cudaStream_t>, std::pair<void*, size_t>> g_ws;  // cached workspaces
+
+struct HostPath {
+    cudaStream_t stream = nullptr;
+    void* d_in = nullptr;
+    size_t in_bytes = 0;
+    float* d_out = nullptr;
+    size_t out_bytes = 0;
+    void* d_ws = nullptr;
+    size_t ws_bytes = 0;
+    std::mutex mu;
+};
+std::map<int, HostPath*> g_host;
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+bool valid_dtype(int d) { return d == NLM_U8 || d == NLM_F16 || d == NLM_F32; }
+size_t dtype_bytes(int d) { return d == NLM_U8 ? 1 : (d == NLM_F16 ? 2 : 4); }
+
+// Grows (never shrinks) a cached device buffer.  Refuses to allocate while the
+// stream is being captured.
+int ensure_buffer(void** ptr, size_t* have, size_t need, cudaStream_t stream) {
+    if (*have >= need && *ptr) return NLM_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (stream) cudaStreamIsCapturing(stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone)
+        return fail(NLM_ERR_WORKSPACE,
+                    "workspace cache must grow (%zu bytes) during stream capture; pass a "
+                    "workspace or warm the cache before capturing",
+                    need);
+    if (*ptr) {
+        cudaStreamSynchronize(stream);
+        cudaFree(*ptr);
+        *ptr = nullptr;
+        *have = 0;
+    }
+    cudaError_t e = cudaMalloc(ptr, need);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return cuda_fail(e, "cudaMalloc(workspace)");
+    }
+    *have = need;
+    return NLM_OK;
+}
+
+// Resolves the workspace: caller-provided or the (device, stream) cache.
+int resolve_ws(void** d_ws, size_t* ws_bytes, size_t need, cudaStream_t stream) {
+    if (*d_ws) {
+        if (*ws_bytes < need)
+            return fail(NLM_ERR_WORKSPACE, "workspace of %zu bytes < %zu required", *ws_bytes,
+                        need);
+        if (reinterpret_cast<uintptr_t>(*d_ws) % kAlign)
+            return fail(NLM_ERR_INVALID_ARG, "workspace must be %zu-byte aligned", kAlign);
+        return NLM_OK;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_mutex);
+    auto& slot = g_ws[{dev, stream}];
+    int rc = ensure_buffer(&slot.first, &slot.second, need, stream);
+    if (rc != NLM_OK) return rc;
+    *d_ws = slot.first;
+    *ws_bytes = slot.second;
+    return NLM_OK;
+}
+
+float weight_scale(int pr, int dims, float h) {
+    const double k = 2.0 * pr + 1.0;
+    const double P = dims == 3 ? k * k * k : k * k;
+    return (float)sqrt(1.4426950408889634 / (P * (double)h * (double)h));
+}
+
+int check_common(const void* in, const void* out, int in_dtype, int sr, int pr, float h,
+                 unsigned int flags) {
+    if (!in || !out) return fail(NLM_ERR_INVALID_ARG, "null input or output pointer");
+    if (!valid_dtype(in_dtype)) return fail(NLM_ERR_INVALID_ARG, "invalid in_dtype %d", in_dtype);
+    if (sr < 0 || pr < 0) return fail(NLM_ERR_INVALID_ARG, "negative radius (sr=%d pr=%d)", sr, pr);
+    if (!(h > 0.f) || !isfinite(h)) return fail(NLM_ERR_INVALID_ARG, "h must be finite and > 0");
+    if (flags & ~(NLM_FLAG_FP16_STORAGE | NLM_FLAG_PREPADDED))
+        return fail(NLM_ERR_INVALID_ARG, "unknown flag bits 0x%x", flags);
+    return NLM_OK;
+}
+
+int check_dims3(int X, int Y, int Z, int H) {
+    if (X < 1 || Y < 1 || Z < 1) return fail(NLM_ERR_INVALID_ARG, "non-positive extent");
+    // staging grid: one block per padded row (grid.y = padded planes <= 65535);
+    // TMA global extents < 2^32; 64-bit element indices everywhere.
+    if ((long long)Z + 2LL * H > 65535 || (long long)Y + 2LL * H > (1LL << 30) ||
+        (long long)X + 2LL * H > (1LL << 30))
+        return fail(NLM_ERR_INVALID_ARG, "volume too large (%d x %d x %d)", X, Y, Z);
+    return NLM_OK;
+}
+
+}  // namespace
+
+unsigned int* device_error_word() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    auto it = g_errword.find(dev);
+    if (it != g_errword.end()) return it->second;
+    unsigned int* p = nullptr;
+    if (cudaGetSymbolAddress((void**)&p, g_device_error_word) != cudaSuccess) return nullptr;
+    g_errword[dev] = p;
+    return p;
+}
+
+cudaError_t encode_tensor_map(CUtensorMap* map, bool fp16, int rank, const uint64_t* dims,
+                              const uint64_t* strides_bytes, const uint32_t* box, void* base) {
+    {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        if (!g_encode) {
+            cudaDriverEntryPointQueryResult q;
+            void* fn = nullptr;
+            cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                             cudaEnableDefault, &q);
+            if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+                return e != cudaSuccess ? e : cudaErrorNotSupported;
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        }
+    }
+    cuuint64_t d[5];
+    cuuint64_t s[4];
+    cuuint32_t b[5], es[5];
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        es[i] = 1;
+        if (i + 1 < rank) s[i] = strides_bytes[i];
+    }
+    CUresult r = g_encode(map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                          (cuuint32_t)rank, base, d, s, b, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace gnlm
+
+using namespace gnlm;
+
+extern "C" {
+
+const char* nlm_version(void) { return "gnlm 0.1 sm_103a"; }
+
+const char* nlm_last_error(void) { return t_last_error; }
+
+int nlm_device_status(unsigned int* flags) {
+    unsigned int* w = device_error_word();
+    if (!w) return fail(NLM_ERR_CUDA, "no device error word (no CUDA device?)");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
+    unsigned int v = 0;
+    e = cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read device error word");
+    const unsigned int zero = 0;
+    e = cudaMemcpy(w, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "clear device error word");
+    if (flags) *flags = v;
+    if (v) return fail(NLM_ERR_DEVICE, "device error word 0x%x", v);
+    return NLM_OK;
+}
+
+int nlm_release_cached(void) {
+    std::lock_guard<std::mutex> lk(g_mutex);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    for (auto& kv : g_ws) {
+        if (kv.second.first) {
+            cudaSetDevice(kv.first.first);
+            cudaStreamSynchronize(kv.first.second);
+            cudaFree(kv.second.first);
+        }
+    }
+    g_ws.clear();
+    for (auto& kv : g_host) {
+        HostPath* hp = kv.second;
+        cudaSetDevice(kv.first);
+        std::lock_guard<std::mutex> hl(hp->mu);
+        if (hp->stream) cudaStreamSynchronize(hp->stream);
+        cudaFree(hp->d_in);
+        cudaFree(hp->d_out);
+        cudaFree(hp->d_ws);
+        hp->d_in = hp->d_out = nullptr;
+        hp->d_ws = nullptr;
+        hp->in_bytes = hp->out_bytes = hp->ws_bytes = 0;
+    }
+    cudaSetDevice(prev);
+    return NLM_OK;
+}
+
+size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags) {
+    if (X < 1 || Y < 1 || Z < 1 || sr < 0 || pr < 0) return 0;
+    const int H = sr + pr;
+    return make_staging(X, Y, Z, H, H, (flags & NLM_FLAG_FP16_STORAGE) != 0).bytes();
+}
+
+static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
+                        float h, unsigned int flags, void** d_ws, size_t* ws_bytes,
+                        cudaStream_t stream) {
+    const int H = sr + pr;
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    if (!nlm3d_fwd_supported(sr, pr, fp16))
+        return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
+    Staging st = make_staging(X, Y, Z, H, H, fp16);
+    int rc = resolve_ws(d_ws, ws_bytes, st.bytes(), stream);
+    if (rc) return rc;
+    cudaError_t e = launch_stage(d_in, in_dtype, (flags & NLM_FLAG_PREPADDED) != 0,
+                                 weight_scale(pr, 3, h), st, *d_ws, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "stage3d launch");
+    return NLM_OK;
+}
+
+static int fwd3d_staged_impl(const void* d_ws, int X, int Y, int Z, int sr, int pr, float h,
+                             float* d_out, float* d_zsum, unsigned int flags,
+                             cudaStream_t stream) {
+    const int H = sr + pr;
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    Staging st = make_staging(X, Y, Z, H, H, fp16);
+    cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, 1.0f / weight_scale(pr, 3, h), d_out,
+                                     d_zsum, device_error_word(), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nlm3d_fwd launch");
+    return NLM_OK;
+}
+
+int nlm3d_stage(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr, float h,
+                unsigned int flags, void* d_ws, size_t ws_bytes, nlm_stream_t stream) {
+    int rc = check_common(d_in, d_ws ? d_ws : d_in, in_dtype, sr, pr, h, flags);
+    if (rc) return rc;
+    if (!d_ws) return fail(NLM_ERR_INVALID_ARG, "nlm3d_stage needs a caller workspace");
+    if ((rc = check_dims3(X, Y, Z, sr + pr))) return rc;
+    return stage3d_impl(d_in, in_dtype, X, Y, Z, sr, pr, h, flags, &d_ws, &ws_bytes,
+                        (cudaStream_t)stream);
+}
+
+int nlm3d_forward_staged(const void* d_ws, size_t ws_bytes, int X, int Y, int Z, int sr, int pr,
+                         float h, float* d_out, float* d_zsum, unsigned int flags,
+                         nlm_stream_t stream) {
+    int rc = check_common(d_ws, d_out, NLM_F32, sr, pr, h, flags);
+    if (rc) return rc;
+    if ((rc = check_dims3(X, Y, Z, sr + pr))) return rc;
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    if (!nlm3d_fwd_supported(sr, pr, fp16))
+        return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
+    const size_t need = nlm3d_workspace_bytes(X, Y, Z, sr, pr, flags);
+    if (ws_bytes < need)
+        return fail(NLM_ERR_WORKSPACE, "staged workspace of %zu bytes < %zu required", ws_bytes,
+                    need);
+    return fwd3d_staged_impl(d_ws, X, Y, Z, sr, pr, h, d_out, d_zsum, flags, (cudaStream_t)stream);
+}
+
+int nlm3d_forward(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr, float h,
+                  float* d_out, float* d_zsum, unsigned int flags, void* d_ws, size_t ws_bytes,
+                  nlm_stream_t stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    int rc = check_common(d_in, d_out, in_dtype, sr, pr, h, flags);
+    if (rc) return rc;
+    if ((rc = check_dims3(X, Y, Z, sr + pr))) return rc;
+    if ((rc = stage3d_impl(d_in, in_dtype, X, Y, Z, sr, pr, h, flags, &d_ws, &ws_bytes, stream)))
+        return rc;
+    return fwd3d_staged_impl(d_ws, X, Y, Z, sr, pr, h, d_out, d_zsum, flags, stream);
+}
+
+size_t nlm2d_workspace_bytes(int X, int Y, int sr, int pr, unsigned int flags) {
+    if (X < 1 || Y < 1 || sr < 0 || pr < 0) return 0;
+    return make_staging(X, Y, 1, sr + pr, 0, (flags & NLM_FLAG_FP16_STORAGE) != 0).bytes();
+}
+
+int nlm2d_forward(const void* d_in, int in_dtype, int X, int Y, int sr, int pr, float h,
+                  float* d_out, float* d_zsum, unsigned int flags, void* d_ws, size_t ws_bytes,
+                  nlm_stream_t stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    int rc = check_common(d_in, d_out, in_dtype, sr, pr, h, flags);
+    if (rc) return rc;
+    const int H = sr + pr;
+    if ((rc = check_dims3(X, Y, 1, H))) return rc;
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    if (!nlm2d_fwd_supported(sr, pr, fp16))
+        return fail(NLM_ERR_UNSUPPORTED, "2D (sr=%d, pr=%d) not compiled in", sr, pr);
+    Staging st = make_staging(X, Y, 1, H, 0, fp16);
+    if ((rc = resolve_ws(&d_ws, &ws_bytes, st.bytes(), stream))) return rc;
+    unsigned int* ew = device_error_word();
+    const float s = weight_scale(pr, 2, h);
+    cudaError_t e = launch_stage(d_in, in_dtype, (flags & NLM_FLAG_PREPADDED) != 0, s, st, d_ws, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "stage2d launch");
+    e = launch_nlm2d_fwd(st, d_ws, sr, pr, fp16, 1.0f / s, d_out, d_zsum, ew, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nlm2d_fwd launch");
+    return NLM_OK;
+}
+
+static HostPath* host_path(int dev) {
+    std::lock_guard<std::mutex> lk(g_mutex);
+    HostPath*& hp = g_host[dev];
+    if (!hp) hp = new HostPath();
+    return hp;
+}
+
+static int host_forward(const void* h_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
+                        float h, float* h_out, unsigned int flags, int dims) {
+    int rc = check_common(h_in, h_out, in_dtype, sr, pr, h, flags);
+    if (rc) return rc;
+    const int H = sr + pr;
+    if ((rc = check_dims3(X, Y, Z, H))) return rc;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    HostPath* hp = host_path(dev);
+    std::lock_guard<std::mutex> lk(hp->mu);
+    if (!hp->stream) {
+        e = cudaStreamCreateWithFlags(&hp->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    }
+    const bool prepadded = (flags & NLM_FLAG_PREPADDED) != 0;
+    const int Hz = dims == 3 ? H : 0;
+    const size_t nin = prepadded ? (size_t)(X + 2 * H) * (Y + 2 * H) * (Z + 2 * Hz)
+                                 : (size_t)X * Y * Z;
+    const size_t in_bytes = nin * dtype_bytes(in_dtype);
+    const size_t out_bytes = (size_t)X * Y * Z * sizeof(float);
+    const size_t ws = dims == 3 ? nlm3d_workspace_bytes(X, Y, Z, sr, pr, flags)
+                                : nlm2d_workspace_bytes(X, Y, sr, pr, flags);
+    if ((rc = ensure_buffer(&hp->d_in, &hp->in_bytes, in_bytes, hp->stream))) return rc;
+    if ((rc = ensure_buffer((void**)&hp->d_out, &hp->out_bytes, out_bytes, hp->stream))) return rc;
+    if ((rc = ensure_buffer(&hp->d_ws, &hp->ws_bytes, ws, hp->stream))) return rc;
+    e = cudaMemcpyAsync(hp->d_in, h_in, in_bytes, cudaMemcpyHostToDevice, hp->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "host->device copy");
+    rc = dims == 3 ? nlm3d_forward(hp->d_in, in_dtype, X, Y, Z, sr, pr, h, hp->d_out, nullptr,
+                                   flags, hp->d_ws, hp->ws_bytes, (nlm_stream_t)hp->stream)
+                   : nlm2d_forward(hp->d_in, in_dtype, X, Y, sr, pr, h, hp->d_out, nullptr, flags,
+                                   hp->d_ws, hp->ws_bytes, (nlm_stream_t)hp->stream);
+    if (rc) return rc;
+    e = cudaMemcpyAsync(h_out, hp->d_out, out_bytes, cudaMemcpyDeviceToHost, hp->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "device->host copy");
+    e = cudaStreamSynchronize(hp->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    return NLM_OK;
+}
+
+int nlm3d_forward_host(const void* h_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
+                       float h, float* h_out, unsigned int flags) {
+    return host_forward(h_in, in_dtype, X, Y, Z, sr, pr, h, h_out, flags, 3);
+}
+
+int nlm2d_forward_host(const void* h_in, int in_dtype, int X, int Y, int sr, int pr, float h,
+                       float* h_out, unsigned int flags) {
+    return host_forward(h_in, in_dtype, X, Y, 1, sr, pr, h, h_out, flags, 2);
+}
+
+}  // extern "C"

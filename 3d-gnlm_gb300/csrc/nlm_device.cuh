@@ -1,0 +1,121 @@
+// Device-side building blocks shared by the NLM kernels (sm_103a):
+// TMA tile loads, mbarrier waits with an iteration limit, the MUFU ex2 weight,
+// and the device error word.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gnlm {
+
+// Bits of the device error word (one 32-bit word per device, see nlm_abi.cu).
+enum : unsigned int {
+    DEVERR_TMA_TIMEOUT = 0x1u,     // a tile load did not complete within the wait limit
+    DEVERR_QUEUE_TIMEOUT = 0x2u,   // a persistent-kernel queue wait gave up
+    DEVERR_BAD_DESC = 0x4u,        // a work item failed its own bounds check
+};
+
+// Upper bound on mbarrier.try_wait polls before a wait gives up.  Each poll may
+// suspend the thread for a hardware-defined interval, so this bounds the wait
+// at well under a second on a healthy device.
+constexpr uint32_t kMaxWaitPolls = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+// Makes the initialised barrier visible to the async (TMA) proxy.
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of `bar` with an iteration limit.  Returns false if
+// the limit ran out (the caller records the error and abandons the tile).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kMaxWaitPolls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// 3D tiled TMA load of one box into shared memory, completing on `bar`.
+// Coordinates are element indices (x innermost); x * sizeof(elem) must be a
+// multiple of 16 bytes, which every caller guarantees by rounding x down.
+__device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// 2^(-x) on the MUFU pipe (PTX ex2.approx.ftz.f32: about 2 ulp; 0 for large x).
+__device__ __forceinline__ float ex2_neg(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-x));
+    return y;
+}
+
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_f32(unsigned char v) { return static_cast<float>(v); }
+
+template <typename T>
+__device__ __forceinline__ T from_f32(float v);
+template <>
+__device__ __forceinline__ float from_f32<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __half from_f32<__half>(float v) { return __float2half_rn(v); }
+
+// OpenCV BORDER_REFLECT_101 for any offset (repeated reflection, period 2n-2).
+__host__ __device__ __forceinline__ int reflect101(int i, int n) {
+    if (n <= 1) return 0;
+    const int period = 2 * n - 2;
+    i %= period;
+    if (i < 0) i += period;
+    return i < n ? i : period - i;
+}
+
+__device__ __forceinline__ void raise_device_error(unsigned int* word, unsigned int bits) {
+    if (word) atomicOr(word, bits);
+}
+
+}  // namespace gnlm

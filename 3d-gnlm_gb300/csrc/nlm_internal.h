@@ -1,0 +1,59 @@
+// Host-side declarations shared by the translation units of libgnlm.so.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace gnlm {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Device-resident staging copy of one volume: REFLECT_101-padded by `H` voxels
+// in x and y and by `Hz` in z (Hz = 0 for 2D), converted to the storage type
+// and pre-multiplied by `scale` = sqrt(log2(e) / (P h^2)) so that the kernels
+// get the base-2 exponent of the weight directly as a sum of squared
+// differences.  Layout [Zp][Yp][Xs], x stride Xs a multiple of 16 bytes (the
+// TMA global-stride rule).
+struct Staging {
+    int X = 0, Y = 0, Z = 0;  // unpadded extents
+    int H = 0, Hz = 0;        // halo in x/y and in z
+    int Xp = 0, Yp = 0, Zp = 0;
+    int Xs = 0;               // x stride in elements
+    int elem = 4;             // 4 (FP32) or 2 (FP16)
+    size_t bytes() const { return align_up((size_t)Xs * Yp * Zp * elem, kAlign); }
+};
+
+Staging make_staging(int X, int Y, int Z, int H, int Hz, bool fp16);
+
+// Pads, converts and scales `in` into `dst` (layout of `st`).  in_dtype is an
+// nlm_dtype; with `prepadded` the input already has the halo (layout
+// [Zp][Yp][Xp], no stride padding) and is copied, converted and scaled only.
+cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float scale,
+                         const Staging& st, void* dst, cudaStream_t stream);
+
+// 3D forward over a staged volume.  Returns cudaErrorNotSupported when the
+// (sr, pr, fp16) combination has no compiled instance.
+cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
+                             float inv_scale, float* out, float* zsum, unsigned int* errword,
+                             cudaStream_t stream);
+bool nlm3d_fwd_supported(int sr, int pr, bool fp16);
+
+// 2D forward over a staged image (Z = 1, Hz = 0).
+cudaError_t launch_nlm2d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
+                             float inv_scale, float* out, float* zsum, unsigned int* errword,
+                             cudaStream_t stream);
+bool nlm2d_fwd_supported(int sr, int pr, bool fp16);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+// dims/strides follow the driver API: dims[0] innermost, strides in bytes for
+// dims 1..rank-1.
+cudaError_t encode_tensor_map(CUtensorMap* map, bool fp16, int rank, const uint64_t* dims,
+                              const uint64_t* strides_bytes, const uint32_t* box, void* base);
+
+// Address of the calling device's error word (see nlm_device_status).
+unsigned int* device_error_word();
+
+}  // namespace gnlm

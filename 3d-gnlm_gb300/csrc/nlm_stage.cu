@@ -1,0 +1,90 @@
+// Staging pass: REFLECT_101 padding + dtype conversion + exponent pre-scaling.
+//
+// Replaces the host-side padding of the reference's driver
+// (3DNLM/nlm.cpp:36-61: copyMakeBorder(BORDER_REFLECT_101) in x/y, slice
+// replication in z; 2D NLM/11x11/nlm.cpp:15-19) with one HBM-streaming kernel
+// that reflects on every axis.  It reads the input once and writes the padded
+// copy once: algorithmic traffic = X*Y*Z*in_bytes + Xs*Yp*Zp*elem.
+#include <cuda_fp16.h>
+
+#include "../../include/nlm.h"
+#include "nlm_device.cuh"
+#include "nlm_internal.h"
+
+namespace gnlm {
+
+Staging make_staging(int X, int Y, int Z, int H, int Hz, bool fp16) {
+    Staging s;
+    s.X = X;
+    s.Y = Y;
+    s.Z = Z;
+    s.H = H;
+    s.Hz = Hz;
+    s.Xp = X + 2 * H;
+    s.Yp = Y + 2 * H;
+    s.Zp = Z + 2 * Hz;
+    s.elem = fp16 ? 2 : 4;
+    const int per16 = 16 / s.elem;
+    s.Xs = (s.Xp + per16 - 1) / per16 * per16;
+    return s;
+}
+
+// One block per padded row (blockIdx.x = row in [0, Yp), blockIdx.y = plane).
+template <typename Tin, typename Tout, bool PREPADDED>
+__global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
+                                                    int Z, int H, int Hz, int Xp, int Yp, int Xs,
+                                                    float scale, Tout* __restrict__ dst) {
+    const int py = blockIdx.x;
+    const int pz = blockIdx.y;
+    Tout* drow = dst + ((size_t)pz * Yp + py) * Xs;
+    const Tin* srow;
+    if (PREPADDED) {
+        srow = in + ((size_t)pz * Yp + py) * Xp;
+    } else {
+        const int sz = reflect101(pz - Hz, Z);
+        const int sy = reflect101(py - H, Y);
+        srow = in + ((size_t)sz * Y + sy) * X;
+    }
+    for (int px = threadIdx.x; px < Xs; px += blockDim.x) {
+        float v = 0.f;
+        if (px < Xp) {
+            const int sx = PREPADDED ? px : reflect101(px - H, X);
+            v = to_f32(srow[sx]) * scale;
+        }
+        drow[px] = from_f32<Tout>(v);
+    }
+}
+
+template <typename Tin, typename Tout>
+static cudaError_t stage_typed(const void* in, bool prepadded, float scale, const Staging& st,
+                               void* dst, cudaStream_t stream) {
+    dim3 grid(st.Yp, st.Zp);
+    const int threads = st.Xs >= 256 ? 256 : (st.Xs >= 128 ? 128 : 64);
+    if (prepadded)
+        stage_kernel<Tin, Tout, true><<<grid, threads, 0, stream>>>(
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Xs, scale, (Tout*)dst);
+    else
+        stage_kernel<Tin, Tout, false><<<grid, threads, 0, stream>>>(
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Xs, scale, (Tout*)dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float scale,
+                         const Staging& st, void* dst, cudaStream_t stream) {
+    const bool fp16 = st.elem == 2;
+    switch (in_dtype) {
+        case NLM_U8:
+            return fp16 ? stage_typed<unsigned char, __half>(in, prepadded, scale, st, dst, stream)
+                        : stage_typed<unsigned char, float>(in, prepadded, scale, st, dst, stream);
+        case NLM_F16:
+            return fp16 ? stage_typed<__half, __half>(in, prepadded, scale, st, dst, stream)
+                        : stage_typed<__half, float>(in, prepadded, scale, st, dst, stream);
+        case NLM_F32:
+            return fp16 ? stage_typed<float, __half>(in, prepadded, scale, st, dst, stream)
+                        : stage_typed<float, float>(in, prepadded, scale, st, dst, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace gnlm

@@ -1,0 +1,212 @@
+"""Python front end of libgnlm.so (the C ABI declared in include/nlm.h).
+
+Every call goes through ctypes into the CUDA library; there is no CPU or
+framework fallback.  If the library is missing, ``lib()`` raises.  PyTorch is
+used only to own device memory and streams: tensors are passed as raw device
+pointers.
+"""
+import ctypes
+import os
+import subprocess
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.dirname(_HERE)
+REPO_DIR = os.path.dirname(PKG_DIR)
+LIB_DIR = os.path.join(PKG_DIR, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libgnlm.so")
+LEGACY_LIB_PATH = os.path.join(LIB_DIR, "libgnlm_legacy.so")
+HEADER_DIR = os.path.join(REPO_DIR, "include")
+
+NLM_OK = 0
+NLM_ERR_INVALID_ARG = -1
+NLM_ERR_UNSUPPORTED = -2
+NLM_ERR_CUDA = -3
+NLM_ERR_WORKSPACE = -4
+NLM_ERR_DEVICE = -5
+NLM_ERR_NO_DEVICE = -6
+
+NLM_U8, NLM_F16, NLM_F32 = 0, 1, 2
+NLM_FLAG_FP16_STORAGE = 0x1
+NLM_FLAG_PREPADDED = 0x2
+
+_lib = None
+
+
+class NLMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"nlm status {code}: {msg}")
+        self.code = code
+
+
+def build(jobs=8, extra_nvflags=None):
+    """Compile libgnlm.so (+ legacy shim and driver) for sm_103a with make."""
+    cmd = ["make", "-s", "-C", PKG_DIR, f"-j{jobs}"]
+    if extra_nvflags:
+        cmd.append(f"EXTRA_NVFLAGS={extra_nvflags}")
+    subprocess.run(cmd, check=True)
+
+
+def lib():
+    """Load libgnlm.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run gnlm.build() (nvcc, sm_103a)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, sz, i, u, f = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint, ctypes.c_float
+    L.nlm_version.restype = ctypes.c_char_p
+    L.nlm_last_error.restype = ctypes.c_char_p
+    L.nlm_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    L.nlm_release_cached.restype = i
+    L.nlm3d_workspace_bytes.argtypes = [i, i, i, i, i, u]
+    L.nlm3d_workspace_bytes.restype = sz
+    L.nlm3d_forward.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp, sz, vp]
+    L.nlm3d_forward_host.argtypes = [vp, i, i, i, i, i, i, f, vp, u]
+    L.nlm3d_stage.argtypes = [vp, i, i, i, i, i, i, f, u, vp, sz, vp]
+    L.nlm3d_forward_staged.argtypes = [vp, sz, i, i, i, i, i, f, vp, vp, u, vp]
+    L.nlm2d_workspace_bytes.argtypes = [i, i, i, i, u]
+    L.nlm2d_workspace_bytes.restype = sz
+    L.nlm2d_forward.argtypes = [vp, i, i, i, i, i, f, vp, vp, u, vp, sz, vp]
+    L.nlm2d_forward_host.argtypes = [vp, i, i, i, i, i, f, vp, u]
+    _lib = L
+    return L
+
+
+def last_error():
+    return lib().nlm_last_error().decode()
+
+
+def check(rc):
+    if rc != NLM_OK:
+        raise NLMError(rc, last_error())
+    return rc
+
+
+def device_status():
+    """(status, flags): reads and clears the device error word (synchronises)."""
+    flags = ctypes.c_uint(0)
+    rc = lib().nlm_device_status(ctypes.byref(flags))
+    return rc, flags.value
+
+
+# ----------------------------------------------------------------- torch glue
+def _torch():
+    import torch
+    return torch
+
+
+def _dtype_code(t):
+    torch = _torch()
+    return {torch.uint8: NLM_U8, torch.float16: NLM_F16, torch.float32: NLM_F32}[t.dtype]
+
+
+def _stream_ptr(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def nlm3d_forward(x, sr, pr, h, fp16_storage=False, prepadded=False, return_zsum=False,
+                  out=None, zsum=None, workspace=None, stream=None, shape=None):
+    """3D NLM of a CUDA tensor [Z, Y, X] (uint8/float16/float32) -> float32 [Z, Y, X].
+
+    With prepadded=True, ``x`` is the reference's padded layout and ``shape``
+    gives the unpadded (Z, Y, X).
+    """
+    torch = _torch()
+    assert x.is_cuda and x.is_contiguous()
+    Z, Y, X = shape if shape is not None else x.shape
+    flags = (NLM_FLAG_FP16_STORAGE if fp16_storage else 0) | (NLM_FLAG_PREPADDED if prepadded else 0)
+    if out is None:
+        out = torch.empty((Z, Y, X), device=x.device, dtype=torch.float32)
+    if return_zsum and zsum is None:
+        zsum = torch.empty((Z, Y, X), device=x.device, dtype=torch.float32)
+    ws_ptr, ws_bytes = None, 0
+    if workspace is not None:
+        ws_ptr, ws_bytes = ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+    check(lib().nlm3d_forward(_ptr(x), _dtype_code(x), X, Y, Z, sr, pr, float(h), _ptr(out),
+                              _ptr(zsum), flags, ws_ptr, ws_bytes, _stream_ptr(stream)))
+    return (out, zsum) if return_zsum else out
+
+
+def nlm3d_workspace_bytes(shape, sr, pr, fp16_storage=False):
+    Z, Y, X = shape
+    return int(lib().nlm3d_workspace_bytes(X, Y, Z, sr, pr,
+                                           NLM_FLAG_FP16_STORAGE if fp16_storage else 0))
+
+
+def nlm3d_stage(x, sr, pr, h, workspace, fp16_storage=False, prepadded=False, stream=None,
+                shape=None):
+    """Stage (pad, convert, pre-scale) ``x`` into the uint8 CUDA tensor ``workspace``."""
+    Z, Y, X = shape if shape is not None else x.shape
+    flags = (NLM_FLAG_FP16_STORAGE if fp16_storage else 0) | (NLM_FLAG_PREPADDED if prepadded else 0)
+    check(lib().nlm3d_stage(_ptr(x), _dtype_code(x), X, Y, Z, sr, pr, float(h), flags,
+                            _ptr(workspace), workspace.numel() * workspace.element_size(),
+                            _stream_ptr(stream)))
+
+
+def nlm3d_forward_staged(workspace, shape, sr, pr, h, out, zsum=None, fp16_storage=False,
+                         stream=None):
+    """Run the fused 3D kernel on a volume staged by nlm3d_stage."""
+    Z, Y, X = shape
+    flags = NLM_FLAG_FP16_STORAGE if fp16_storage else 0
+    check(lib().nlm3d_forward_staged(_ptr(workspace), workspace.numel() * workspace.element_size(),
+                                     X, Y, Z, sr, pr, float(h), _ptr(out), _ptr(zsum), flags,
+                                     _stream_ptr(stream)))
+    return out
+
+
+def nlm2d_forward(x, sr, pr, h, fp16_storage=False, prepadded=False, return_zsum=False,
+                  out=None, zsum=None, workspace=None, stream=None, shape=None):
+    """2D NLM of a CUDA tensor [Y, X] -> float32 [Y, X]."""
+    torch = _torch()
+    assert x.is_cuda and x.is_contiguous()
+    Y, X = shape if shape is not None else x.shape
+    flags = (NLM_FLAG_FP16_STORAGE if fp16_storage else 0) | (NLM_FLAG_PREPADDED if prepadded else 0)
+    if out is None:
+        out = torch.empty((Y, X), device=x.device, dtype=torch.float32)
+    if return_zsum and zsum is None:
+        zsum = torch.empty((Y, X), device=x.device, dtype=torch.float32)
+    ws_ptr, ws_bytes = None, 0
+    if workspace is not None:
+        ws_ptr, ws_bytes = ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+    check(lib().nlm2d_forward(_ptr(x), _dtype_code(x), X, Y, sr, pr, float(h), _ptr(out),
+                              _ptr(zsum), flags, ws_ptr, ws_bytes, _stream_ptr(stream)))
+    return (out, zsum) if return_zsum else out
+
+
+def _np_dtype_code(a):
+    import numpy as np
+    return {np.dtype(np.uint8): NLM_U8, np.dtype(np.float16): NLM_F16,
+            np.dtype(np.float32): NLM_F32}[a.dtype]
+
+
+def nlm3d_forward_host(a, sr, pr, h, fp16_storage=False, prepadded=False, shape=None, out=None):
+    """Host-buffer 3D form (numpy in, numpy out; synchronous)."""
+    import numpy as np
+    a = np.ascontiguousarray(a)
+    Z, Y, X = shape if shape is not None else a.shape
+    flags = (NLM_FLAG_FP16_STORAGE if fp16_storage else 0) | (NLM_FLAG_PREPADDED if prepadded else 0)
+    if out is None:
+        out = np.empty((Z, Y, X), np.float32)
+    check(lib().nlm3d_forward_host(a.ctypes.data_as(ctypes.c_void_p), _np_dtype_code(a), X, Y, Z,
+                                   sr, pr, float(h), out.ctypes.data_as(ctypes.c_void_p), flags))
+    return out
+
+
+def nlm2d_forward_host(a, sr, pr, h, fp16_storage=False, prepadded=False, shape=None, out=None):
+    """Host-buffer 2D form (numpy in, numpy out; synchronous)."""
+    import numpy as np
+    a = np.ascontiguousarray(a)
+    Y, X = shape if shape is not None else a.shape
+    flags = (NLM_FLAG_FP16_STORAGE if fp16_storage else 0) | (NLM_FLAG_PREPADDED if prepadded else 0)
+    if out is None:
+        out = np.empty((Y, X), np.float32)
+    check(lib().nlm2d_forward_host(a.ctypes.data_as(ctypes.c_void_p), _np_dtype_code(a), X, Y, sr,
+                                   pr, float(h), out.ctypes.data_as(ctypes.c_void_p), flags))
+    return out

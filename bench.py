@@ -1,0 +1,355 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 NLM denoiser on the 3D 256^3 workload.
+
+Workload: one 256x256x256 float32 volume (64 seeded ellipsoids, sigma 0.05),
+search 7^3 (sr 3), patch 3^3 (pr 1), h 0.05.  A step is one forward pass over
+the volume: the staging pass (REFLECT_101 pad + pre-scale) and the fused NLM
+kernel, input resident in HBM.  Between timed steps a 256 MiB buffer is
+written to flush the 129 MB L2.  ``value`` is Mvoxel/s of the plain FP32 form;
+the FP16-storage form is reported beside it.  ``e2e`` is the same metric through
+the host-buffer C-ABI call (nlm3d_forward_host) with the host<->device copies
+inside the timed region.
+
+``--impl reference`` times the reference's path on the host cores instead.  The
+reference ships no CPU implementation of NLM (its nlm.cpp only calls the GPU),
+so that arm runs the oracle's FP32 separable restatement of the reference's
+arithmetic with every host thread, on a bounded z-slab sample of the same
+volume per step.
+
+Multi-GPU: the path does not shard; under torchrun every rank denoises its own
+replica and ``value`` sums the ranks' voxels over the slowest rank's time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "3d-gnlm_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mvoxel/s 3D NLM 256³ S7³ P3³ (fp32 vs fp16-store/batched); fwd+adjoint ms"
+UNIT = "Mvoxel/s"
+SHAPE = (256, 256, 256)
+SR, PR, H = 3, 1, 0.05
+N_ELLIPSOIDS, SIGMA, SEED = 64, 0.05, 2
+OFFSETS = (2 * SR + 1) ** 3
+FLOPS_PER_PAIR = 12  # diff, square, 6 box-sum add/sub, scale, Z add, num FMA (2)
+L2_FLUSH_BYTES = 256 << 20
+WORKLOAD_NAME = "nlm3d_256cubed_sr3_pr1_fp32"
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def fp32_peak_tflops(torch):
+    """FP32 FMA throughput of this GPU, measured by the probe kernel (best of 3)."""
+    import gnlm
+    path = os.path.join(gnlm.LIB_DIR, "libgnlm_probe.so")
+    P = ctypes.CDLL(path)
+    P.gnlm_probe_fp32.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    P.gnlm_probe_fp32_flops.argtypes = [ctypes.c_int, ctypes.c_int]
+    P.gnlm_probe_fp32_flops.restype = ctypes.c_double
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sms * 8, 2048
+    buf = torch.empty(blocks, device="cuda")
+    s = torch.cuda.current_stream()
+    best = 0.0
+    for i in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        P.gnlm_probe_fp32(ctypes.c_void_p(buf.data_ptr()), blocks, iters,
+                          ctypes.c_void_p(s.cuda_stream))
+        e1.record()
+        e1.synchronize()
+        if i > 0:
+            best = max(best, P.gnlm_probe_fp32_flops(blocks, iters) / (e0.elapsed_time(e1) * 1e-3))
+    return best / 1e12
+
+
+def read_profile_traffic(kernel_key):
+    """Per-launch DRAM bytes of a kernel from profiles/traffic.txt (ncu capture)."""
+    path = os.path.join(REPO, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel_key:
+            return float(parts[2])
+    return None
+
+
+def cpu_baseline(shape, budget_s=10.0):
+    """Oracle FP32 separable form on a z-slab of the workload, all host threads."""
+    import oracle as O
+    from gnlm import phantom
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    Z, Y, X = shape
+    vol, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=N_ELLIPSOIDS, sigma=SIGMA, seed=SEED)
+    nz = 4
+    t0 = time.perf_counter()
+    O.nlm3d(np.ascontiguousarray(vol[:nz]), SR, PR, H)
+    dt = time.perf_counter() - t0
+    rate = nz * Y * X / dt
+    nz = int(min(Z, max(4, budget_s * rate / (Y * X))))
+    slab = np.ascontiguousarray(vol[Z // 2 - nz // 2:Z // 2 - nz // 2 + nz])
+    t0 = time.perf_counter()
+    O.nlm3d(slab, SR, PR, H)
+    dt = time.perf_counter() - t0
+    return {"value": round(nz * Y * X / dt / 1e6, 3), "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"z-slab {nz}x{Y}x{X} of the 256^3 volume, oracle FP32 separable form "
+                      f"(reflect borders at the slab ends), {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    import oracle as O
+    from gnlm import phantom
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    vol, _ = phantom.ellipsoid_phantom(SHAPE, n_ellipsoids=N_ELLIPSOIDS, sigma=SIGMA, seed=SEED)
+    Z, Y, X = SHAPE
+    nz = 8
+    slab = np.ascontiguousarray(vol[Z // 2 - nz // 2:Z // 2 + nz // 2])
+    for _ in range(args.warmup):
+        O.nlm3d(slab, SR, PR, H)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.nlm3d(slab, SR, PR, H)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = nz * Y * X / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "shape": list(SHAPE), "search_radius": SR,
+                   "patch_radius": PR, "h": H, "sample": f"z-slab {nz}x{Y}x{X} per step"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"z-slab {nz}x{Y}x{X} of the 256^3 volume per step; the "
+                                   "reference has no CPU NLM, this is the oracle's FP32 "
+                                   "separable restatement of its arithmetic"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gnlm(args):
+    import torch
+    import gnlm
+    from gnlm import phantom
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    gnlm.lib()
+
+    vol, _ = phantom.ellipsoid_phantom(SHAPE, n_ellipsoids=N_ELLIPSOIDS, sigma=SIGMA, seed=SEED)
+    Z, Y, X = SHAPE
+    nvox = Z * Y * X
+    x = torch.from_numpy(vol).cuda()
+    out = torch.empty_like(x)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed_form(fp16, steps, warmup):
+        ws = torch.empty(gnlm.nlm3d_workspace_bytes(SHAPE, SR, PR, fp16), dtype=torch.uint8,
+                         device="cuda")
+        for _ in range(warmup):
+            gnlm.nlm3d_stage(x, SR, PR, H, ws, fp16_storage=fp16)
+            gnlm.nlm3d_forward_staged(ws, SHAPE, SR, PR, H, out, fp16_storage=fp16)
+        torch.cuda.synchronize()
+        ev = []
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            gnlm.nlm3d_stage(x, SR, PR, H, ws, fp16_storage=fp16)
+            e1.record(stream)
+            gnlm.nlm3d_forward_staged(ws, SHAPE, SR, PR, H, out, fp16_storage=fp16)
+            e2.record(stream)
+            ev.append((e0, e1, e2))
+        torch.cuda.synchronize()
+        step_ms = [a.elapsed_time(c) for a, b, c in ev]
+        stage_ms = [a.elapsed_time(b) for a, b, c in ev]
+        fused_ms = [b.elapsed_time(c) for a, b, c in ev]
+        return step_ms, stage_ms, fused_ms, ws
+
+    # warm-up + the timed FP32 region, bracketed by barrier + synchronize
+    sampler = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    step_ms, stage_ms, fused_ms, ws32 = timed_form(False, args.steps, args.warmup)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * nvox / (ms_per_step * 1e-3) / 1e6
+    out32 = out.clone()
+
+    # FP16-storage form (same loop)
+    s16, st16, f16, _ = timed_form(True, max(3, args.steps // 2), max(3, args.warmup))
+    out16 = out.clone()
+    fp16_value = nvox / (statistics.mean(s16) * 1e-3) / 1e6
+
+    # end-to-end through the host-buffer C-ABI call (pinned host memory)
+    h_in = torch.from_numpy(vol).pin_memory()
+    h_out = torch.empty(SHAPE, dtype=torch.float32).pin_memory()
+    a_in, a_out = h_in.numpy(), h_out.numpy()
+    for _ in range(max(1, args.warmup)):
+        gnlm.nlm3d_forward_host(a_in, SR, PR, H, out=a_out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gnlm.nlm3d_forward_host(a_in, SR, PR, H, out=a_out)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_value = nvox / e2e_s / 1e6
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_value = world * nvox / float(t.item()) / 1e6
+    assert np.array_equal(a_out, out32.cpu().numpy()), "host path disagrees with device path"
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    # accuracy against the FP64 oracle on spot blocks (corners + interior)
+    import oracle as O
+    o32, o16 = out32.cpu().numpy(), out16.cpu().numpy()
+    err32 = err16 = 0.0
+    for (z0, y0, x0) in [(0, 0, 0), (248, 248, 248), (124, 60, 200), (40, 180, 8)]:
+        ref = O.nlm3d_region(vol, SR, PR, H, (z0, y0, x0), (8, 8, 8))
+        err32 = max(err32, float(np.abs(o32[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8] - ref).max()))
+        err16 = max(err16, float(np.abs(o16[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8] - ref).max()))
+
+    peak = fp32_peak_tflops(torch)
+    fused_mean = statistics.mean(fused_ms)
+    achieved = FLOPS_PER_PAIR * OFFSETS * nvox / (fused_mean * 1e-3) / 1e12
+    traffic = read_profile_traffic("nlm3d_fwd_kernel")
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "shape": list(SHAPE), "search_radius": SR,
+                   "patch_radius": PR, "h": H, "phantom": f"{N_ELLIPSOIDS} ellipsoids, sigma {SIGMA}",
+                   "l2": "256 MiB buffer written between timed steps"},
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT,
+                "h2d_bytes_per_step": int(vol.nbytes), "d2h_bytes_per_step": int(vol.nbytes)},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
+                     "peak": round(peak, 3), "unit": "TFLOP/s",
+                     "frac": round(achieved / peak, 4) if peak else None,
+                     "traffic": traffic,
+                     "kernel": "nlm3d_fwd_kernel<3,1,float>",
+                     "peak_source": "FFMA probe kernel measured in this run (FP32 pipe; "
+                                    "MEASURED_PEAKS.json has HBM and bf16 only)",
+                     "algorithmic": f"{FLOPS_PER_PAIR} flops x {OFFSETS} offsets x {nvox} voxels"},
+        "kernels_ms": {"stage": round(statistics.mean(stage_ms), 4),
+                       "fused_fp32": round(fused_mean, 4),
+                       "fused_fp16": round(statistics.mean(f16), 4)},
+        "forms": {"fp32": {"value": round(value, 2), "max_abs_err_vs_fp64": err32},
+                  "fp16_storage": {"value": round(fp16_value, 2), "max_abs_err_vs_fp64": err16}},
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(SHAPE)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gnlm", "reference"], default="gnlm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gnlm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

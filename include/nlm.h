@@ -1,0 +1,141 @@
+/*
+ * nlm.h - C ABI of the GB300 (sm_103a) non-local-means denoiser.
+ *
+ * One shared library (libgnlm.so) exports these entry points.  Every argument is
+ * a plain pointer, size or scalar; no C++ or framework types cross the boundary.
+ *
+ * Conventions
+ *   - Volumes are dense, x fastest: index = (z * Y + y) * X + x.  Images are
+ *     [Y][X].  Inputs are UNPADDED: borders are handled as OpenCV
+ *     BORDER_REFLECT_101 (gfedcb|abcdefgh|gfedcba) on every axis, the padding the
+ *     reference's driver applies before calling its kernels
+ *     (3DNLM/nlm.cpp:36-41, 2D NLM/11x11/nlm.cpp:15-19).  With NLM_FLAG_PREPADDED
+ *     the input is instead the reference's pre-padded layout (halo
+ *     (SS+NS-2)/2 = sr+pr on every side), used as given.
+ *   - sr is the search radius m (search window SS = 2m+1), pr the patch radius n
+ *     (patch NS = 2n+1), h the filtering parameter: w = exp(-(D / NS^d) / h^2),
+ *     D the summed squared patch difference (3DNLM/main.cu:108-109).  The centre
+ *     offset is included; out = sum(w v) / sum(w) (3DNLM/main.cu:110-111,125).
+ *   - d_* pointers are device memory owned by the caller; h_* pointers are host
+ *     memory (pinned is fastest).  Calls are asynchronous on `stream` unless they
+ *     say otherwise.
+ *   - Return value: NLM_OK (0) or a negative nlm_status.  Nothing aborts or
+ *     exits; nlm_last_error() gives the calling thread's last message.
+ *   - Scratch: each forward call needs a workspace.  Pass d_ws/ws_bytes (size
+ *     from the *_workspace_bytes query), or d_ws = NULL to use a buffer the
+ *     library caches per (device, stream) and grows with cudaMalloc; the cache
+ *     grows only outside stream capture, so warm it before capturing.
+ *   - Thread safety: calls are thread-safe; calls on different streams with the
+ *     library cache use different buffers.
+ */
+#ifndef GNLM_NLM_H
+#define GNLM_NLM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t (struct CUstream_st*); NULL is the legacy stream. */
+typedef struct CUstream_st* nlm_stream_t;
+
+typedef enum nlm_status {
+    NLM_OK = 0,
+    NLM_ERR_INVALID_ARG = -1,  /* null pointer, non-positive size, h <= 0, ... */
+    NLM_ERR_UNSUPPORTED = -2,  /* (sr, pr, dtype) combination not compiled in */
+    NLM_ERR_CUDA = -3,         /* a CUDA runtime/driver call failed */
+    NLM_ERR_WORKSPACE = -4,    /* caller workspace smaller than required */
+    NLM_ERR_DEVICE = -5,       /* a kernel raised its device-side error word */
+    NLM_ERR_NO_DEVICE = -6     /* no CUDA device / not an sm_103 device */
+} nlm_status;
+
+/* Element type of an input volume. */
+typedef enum nlm_dtype {
+    NLM_U8 = 0,   /* unsigned char, as the reference's input (3DNLM/main.h:6) */
+    NLM_F16 = 1,  /* IEEE binary16 */
+    NLM_F32 = 2   /* IEEE binary32 */
+} nlm_dtype;
+
+/* Flags for the forward calls. */
+#define NLM_FLAG_FP16_STORAGE 0x1u /* precision form: volume staged as FP16, FP32
+                                      distances, Kahan-compensated weight sums */
+#define NLM_FLAG_PREPADDED 0x2u    /* input is already padded by sr+pr per side */
+
+/* Library identification, e.g. "gnlm 0.1 sm_103a". */
+const char* nlm_version(void);
+
+/* Message of the calling thread's last failing call ("" if none). */
+const char* nlm_last_error(void);
+
+/* Synchronises the current device, then reads and clears the device-side error
+ * word that kernels set when a bounded wait gives up.  *flags receives the word
+ * (0 = no error).  Returns NLM_OK, or NLM_ERR_DEVICE when the word was set. */
+int nlm_device_status(unsigned int* flags);
+
+/* Frees the library-cached workspaces and host-path buffers of every device. */
+int nlm_release_cached(void);
+
+/* ---------------------------------------------------------------- 3D ------ */
+
+/* Bytes of scratch nlm3d_forward needs for this shape (0 on invalid input). */
+size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags);
+
+/*
+ * 3D NLM of one volume: d_in (X*Y*Z elements of in_dtype; with
+ * NLM_FLAG_PREPADDED (X+2H)*(Y+2H)*(Z+2H), H = sr+pr) -> d_out (X*Y*Z floats).
+ * d_zsum (nullable) receives the per-voxel weight sum Z_p, which the adjoint
+ * takes.  Replaces the device part of NLMeansProcessor::NL_Means
+ * (3DNLM/main.h:6, 3DNLM/main.cu:7607-7680): its four kernel variants x 10 runs
+ * become one staging pass and one fused kernel; allocation moves to the caller.
+ */
+int nlm3d_forward(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
+                  float h, float* d_out, float* d_zsum, unsigned int flags, void* d_ws,
+                  size_t ws_bytes, nlm_stream_t stream);
+
+/*
+ * The two halves of nlm3d_forward, for callers that reuse one staged volume
+ * (several outputs, the adjoint) or time the fused kernel alone.
+ * nlm3d_stage writes the padded, converted, pre-scaled volume into d_ws (at
+ * least nlm3d_workspace_bytes); nlm3d_forward_staged runs the fused NLM kernel
+ * on it.  Same (sr, pr, h, flags) must be given to both.  Replace the
+ * H2D-then-launch sequence of 3DNLM/main.cu:7620-7634.
+ */
+int nlm3d_stage(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr, float h,
+                unsigned int flags, void* d_ws, size_t ws_bytes, nlm_stream_t stream);
+int nlm3d_forward_staged(const void* d_ws, size_t ws_bytes, int X, int Y, int Z, int sr, int pr,
+                         float h, float* d_out, float* d_zsum, unsigned int flags,
+                         nlm_stream_t stream);
+
+/*
+ * Host-buffer form with the reference's calling semantics: synchronous, host
+ * pointers in and out, device memory owned by the library (cached per device).
+ * The host->device copy, the kernels and the device->host copy run in order on a
+ * library stream; returns when h_out is written.  This is what
+ * NLMeansProcessor::NL_Means(unsigned char*, float*) (3DNLM/main.h:6) does.
+ */
+int nlm3d_forward_host(const void* h_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
+                       float h, float* h_out, unsigned int flags);
+
+/* ---------------------------------------------------------------- 2D ------ */
+
+size_t nlm2d_workspace_bytes(int X, int Y, int sr, int pr, unsigned int flags);
+
+/*
+ * 2D NLM of one image [Y][X].  Replaces the device part of the 2D
+ * NLMeansProcessor::NL_Means (2D NLM/11x11/main.h:6, 2D NLM/11x11/main.cu:472-539),
+ * whose kernels only support an 11x11 patch; here any compiled (sr, pr).
+ */
+int nlm2d_forward(const void* d_in, int in_dtype, int X, int Y, int sr, int pr, float h,
+                  float* d_out, float* d_zsum, unsigned int flags, void* d_ws,
+                  size_t ws_bytes, nlm_stream_t stream);
+
+/* Host-buffer 2D form (2D NLM/11x11/main.h:6 semantics; synchronous). */
+int nlm2d_forward_host(const void* h_in, int in_dtype, int X, int Y, int sr, int pr, float h,
+                       float* h_out, unsigned int flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GNLM_NLM_H */

@@ -1,0 +1,194 @@
+"""GPU parity tests of the forward kernels through the C ABI.
+
+Bars: plain FP32 form within 1e-5 max abs of the FP32 oracle (the CPU
+restatement of the reference's arithmetic) on data in [0, 1]; the error against
+the FP64 oracle is asserted with the same bound.  FP16-storage form within 1e-3
+max abs of the FP64 oracle.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from gnlm import phantom
+
+pytestmark = pytest.mark.gpu
+
+TOL_F32 = 1e-5
+TOL_F16 = 1e-3
+
+
+def _gpu3d(torch, gnlm, v, sr, pr, h, **kw):
+    x = torch.from_numpy(np.ascontiguousarray(v)).cuda()
+    r = gnlm.nlm3d_forward(x, sr, pr, h, **kw)
+    if isinstance(r, tuple):
+        return tuple(t.cpu().numpy() for t in r)
+    return r.cpu().numpy()
+
+
+def _gpu2d(torch, gnlm, v, sr, pr, h, **kw):
+    x = torch.from_numpy(np.ascontiguousarray(v)).cuda()
+    r = gnlm.nlm2d_forward(x, sr, pr, h, **kw)
+    if isinstance(r, tuple):
+        return tuple(t.cpu().numpy() for t in r)
+    return r.cpu().numpy()
+
+
+def test_3d_64cubed_workload(torch_cuda, gnlm_lib):
+    """64^3, 8 ellipsoids, sigma 0.05, search 7^3, patch 3^3, h 0.05."""
+    v, _ = phantom.ellipsoid_phantom((64, 64, 64), n_ellipsoids=8, sigma=0.05, seed=0)
+    g = _gpu3d(torch_cuda, gnlm_lib, v, 3, 1, 0.05)
+    o32 = O.nlm3d(v, 3, 1, 0.05)
+    o64 = O.nlm3d(v, 3, 1, 0.05, dtype=np.float64)
+    assert np.abs(g - o32).max() <= TOL_F32
+    assert np.abs(g - o64).max() <= TOL_F32
+    assert gnlm_lib.device_status() == (0, 0)
+
+
+SHAPES = [(1, 1, 1), (2, 3, 5), (5, 9, 31), (8, 17, 30), (7, 31, 33), (13, 40, 61), (9, 20, 95)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("sr,pr", [(3, 1), (1, 1), (5, 1), (2, 1), (3, 2)])
+def test_3d_shapes_and_radii(torch_cuda, gnlm_lib, shape, sr, pr):
+    v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=4, sigma=0.05, seed=sum(shape),
+                                     radii=(1.0, 6.0))
+    h = 0.05
+    g, gz = _gpu3d(torch_cuda, gnlm_lib, v, sr, pr, h, return_zsum=True)
+    o, oz = O.nlm3d(v, sr, pr, h, dtype=np.float64, form=O.FORM_SEPARABLE, return_z=True)
+    assert np.abs(g - o).max() <= TOL_F32
+    assert np.abs(gz / oz - 1).max() <= 1e-5
+
+
+@pytest.mark.parametrize("sr,pr", [(3, 1), (5, 1)])
+def test_3d_fp16_storage(torch_cuda, gnlm_lib, sr, pr):
+    v, _ = phantom.ellipsoid_phantom((24, 40, 70), n_ellipsoids=8, sigma=0.05, seed=11)
+    g = _gpu3d(torch_cuda, gnlm_lib, v, sr, pr, 0.05, fp16_storage=True)
+    o = O.nlm3d(v, sr, pr, 0.05, dtype=np.float64)
+    assert np.abs(g - o).max() <= TOL_F16
+
+
+def test_3d_input_dtypes(torch_cuda, gnlm_lib):
+    rng = np.random.default_rng(12)
+    u8 = rng.integers(0, 256, (12, 33, 45), dtype=np.uint8)
+    g = _gpu3d(torch_cuda, gnlm_lib, u8, 3, 1, 10.0)
+    o = O.nlm3d(u8.astype(np.float64), 3, 1, 10.0, dtype=np.float64)
+    assert np.abs(g - o).max() <= TOL_F32 * 255
+    v, _ = phantom.ellipsoid_phantom((12, 33, 45), sigma=0.05, seed=13)
+    f16 = v.astype(np.float16)
+    g = _gpu3d(torch_cuda, gnlm_lib, f16, 3, 1, 0.05)
+    o = O.nlm3d(f16.astype(np.float64), 3, 1, 0.05, dtype=np.float64)
+    assert np.abs(g - o).max() <= TOL_F32
+
+
+def test_3d_prepadded_reference_layout(torch_cuda, gnlm_lib):
+    """The reference driver's input: one uchar slice padded REFLECT_101 in x/y and
+    replicated over depth+SS+NS-2 planes (3DNLM/nlm.cpp:36-61)."""
+    SS, NS = 7, 3
+    X, Y, Z = 40, 36, 16
+    pad = (SS + NS - 2) // 2
+    img = np.random.default_rng(14).integers(0, 256, (Y, X), dtype=np.uint8)
+    p2 = O.pad_reflect101(img, pad)
+    padded = np.ascontiguousarray(np.broadcast_to(p2, (Z + 2 * pad,) + p2.shape))
+    g = _gpu3d(torch_cuda, gnlm_lib, padded, 3, 1, 10.0, prepadded=True, shape=(Z, Y, X))
+    o = O.nlm3d_padded_u8(padded, X, Y, Z, SS, NS, 10.0)
+    assert np.abs(g - o).max() <= TOL_F32 * 255
+
+
+def test_3d_host_path_and_workspace_forms_agree(torch_cuda, gnlm_lib):
+    torch = torch_cuda
+    v, _ = phantom.ellipsoid_phantom((20, 30, 50), sigma=0.05, seed=15)
+    a = _gpu3d(torch, gnlm_lib, v, 3, 1, 0.05)
+    b = gnlm_lib.nlm3d_forward_host(v, 3, 1, 0.05)
+    assert np.array_equal(a, b)
+    nbytes = gnlm_lib.lib().nlm3d_workspace_bytes(50, 30, 20, 3, 1, 0)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    x = torch.from_numpy(v).cuda()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        c = gnlm_lib.nlm3d_forward(x, 3, 1, 0.05, workspace=ws, stream=s)
+    s.synchronize()
+    assert np.array_equal(a, c.cpu().numpy())
+    too_small = torch.empty(nbytes - 256, dtype=torch.uint8, device="cuda")
+    with pytest.raises(gnlm_lib.NLMError) as ei:
+        gnlm_lib.nlm3d_forward(x, 3, 1, 0.05, workspace=too_small)
+    assert ei.value.code == gnlm_lib.NLM_ERR_WORKSPACE
+    assert gnlm_lib.device_status() == (0, 0)
+
+
+def test_3d_256cubed_spot_checks(torch_cuda, gnlm_lib):
+    """Full-size 256^3 (64 ellipsoids): corners, edges and random interior
+    blocks against the FP64 direct oracle; FP16 storage on the same blocks."""
+    v, _ = phantom.ellipsoid_phantom((256, 256, 256), n_ellipsoids=64, sigma=0.05, seed=2)
+    g32 = _gpu3d(torch_cuda, gnlm_lib, v, 3, 1, 0.05)
+    g16 = _gpu3d(torch_cuda, gnlm_lib, v, 3, 1, 0.05, fp16_storage=True)
+    rng = np.random.default_rng(16)
+    boxes = [(0, 0, 0), (248, 248, 248), (0, 248, 120), (248, 0, 0), (100, 255 - 8, 0)]
+    boxes += [tuple(int(c) for c in rng.integers(0, 248, 3)) for _ in range(4)]
+    for (z0, y0, x0) in boxes:
+        o = O.nlm3d_region(v, 3, 1, 0.05, (z0, y0, x0), (8, 8, 8))
+        assert np.abs(g32[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8] - o).max() <= TOL_F32
+        assert np.abs(g16[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8] - o).max() <= TOL_F16
+    assert np.isfinite(g32).all() and np.isfinite(g16).all()
+
+
+def test_2d_2048_workload(torch_cuda, gnlm_lib):
+    """2048^2, 32 discs/rectangles, sigma 0.08, search 11^2, patch 5^2, h 0.08."""
+    im, _ = phantom.disc_rect_phantom((2048, 2048), n_shapes=32, sigma=0.08, seed=0)
+    g = _gpu2d(torch_cuda, gnlm_lib, im, 5, 2, 0.08)
+    o32 = O.nlm2d(im, 5, 2, 0.08)
+    assert np.abs(g - o32).max() <= TOL_F32
+    o64 = O.nlm2d(im, 5, 2, 0.08, dtype=np.float64)
+    assert np.abs(g - o64).max() <= TOL_F32
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (3, 7), (31, 29), (64, 100), (130, 77)])
+@pytest.mark.parametrize("sr,pr", [(5, 2), (3, 1), (1, 1), (7, 2), (3, 5)])
+def test_2d_shapes_and_radii(torch_cuda, gnlm_lib, shape, sr, pr):
+    im, _ = phantom.disc_rect_phantom(shape, n_shapes=6, sigma=0.08, seed=sum(shape))
+    g, gz = _gpu2d(torch_cuda, gnlm_lib, im, sr, pr, 0.08, return_zsum=True)
+    o, oz = O.nlm2d(im, sr, pr, 0.08, dtype=np.float64, return_z=True)
+    assert np.abs(g - o).max() <= TOL_F32
+    assert np.abs(gz / oz - 1).max() <= 1e-5
+
+
+def test_2d_fp16_and_prepadded(torch_cuda, gnlm_lib):
+    im, _ = phantom.disc_rect_phantom((96, 96), sigma=0.08, seed=18)
+    g = _gpu2d(torch_cuda, gnlm_lib, im, 5, 2, 0.08, fp16_storage=True)
+    assert np.abs(g - O.nlm2d(im, 5, 2, 0.08, dtype=np.float64)).max() <= TOL_F16
+    # reference 2D driver layout: REFLECT_101-padded uchar, search 7, patch 11
+    img = np.random.default_rng(19).integers(0, 256, (64, 64), dtype=np.uint8)
+    padded = np.ascontiguousarray(O.pad_reflect101(img, 3 + 5))
+    g = _gpu2d(torch_cuda, gnlm_lib, padded, 3, 5, 10.0, prepadded=True, shape=(64, 64))
+    o = O.nlm2d_padded_u8(padded, 64, 64, 7, 11, 10.0)
+    assert np.abs(g - o).max() <= TOL_F32 * 255
+
+
+def test_legacy_driver_binary(torch_cuda, gnlm_lib, tmp_path):
+    """The raw-array nlm driver (reference 3DNLM/nlm.cpp flow) through the
+    NLMeansProcessor shim: output.bin header and truncated uchar voxels."""
+    exe = os.path.join(gnlm_lib.LIB_DIR, "nlm_legacy")
+    X = Y = Z = 64
+    img = np.random.default_rng(20).integers(0, 256, (Y, X), dtype=np.uint8)
+    src = tmp_path / "in.raw"
+    img.tofile(src)
+    dst = tmp_path / "output.bin"
+    subprocess.run([exe, str(src), str(dst)], check=True, timeout=120)
+    raw = np.fromfile(dst, dtype=np.uint8)
+    hdr = np.frombuffer(raw[:12].tobytes(), dtype=np.int32)
+    assert list(hdr) == [Z, Y, X]
+    got = raw[12:].reshape(Z, Y, X)
+    pad = 4
+    p2 = O.pad_reflect101(img, pad)
+    padded = np.ascontiguousarray(np.broadcast_to(p2, (Z + 2 * pad,) + p2.shape))
+    ref = O.nlm3d_padded_u8(padded, X, Y, Z, 7, 3, 10.0).astype(np.uint8)
+    mismatch = np.count_nonzero(got != ref)
+    assert mismatch <= 0.001 * got.size  # float->uchar truncation at integer boundaries
+    assert np.abs(got.astype(int) - ref.astype(int)).max() <= 1
+
+
+def test_device_status_clean(torch_cuda, gnlm_lib):
+    assert gnlm_lib.device_status() == (0, 0)
