@@ -11,7 +11,8 @@
 // whose y slide hard-codes an 11-wide patch (2D NLM/11x11/main.cu:446), any
 // compiled (sr, pr) is exact.
 //
-// Algorithmic work per (pixel, offset): 10 FP32 flops + 1 exp (see DESIGN).
+// Algorithmic work per (pixel, offset): 10 FP32 flops (diff, square, 2 box-sum
+// add/sub per axis, scale, weight-sum add, weighted-value FMA) + 1 exp.
 #include <cuda_fp16.h>
 
 #include "nlm_device.cuh"

@@ -20,7 +20,8 @@
 //     ex2 gives exp(-(D/P)/h^2) (3DNLM/main.cu:108-109).  num += w v, Z += w
 //     (3DNLM/main.cu:110-111); out = num / Z (3DNLM/main.cu:125).
 //
-// Algorithmic work per (voxel, offset): 12 FP32 flops + 1 exp (see DESIGN).
+// Algorithmic work per (voxel, offset): 12 FP32 flops (diff, square, 2 box-sum
+// add/sub per axis, scale, weight-sum add, weighted-value FMA) + 1 exp.
 #include <cuda_fp16.h>
 
 #include "nlm_device.cuh"
