@@ -135,6 +135,8 @@ int check_dims3(int X, int Y, int Z, int H) {
 
 }  // namespace
 
+int report_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 unsigned int* device_error_word() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;

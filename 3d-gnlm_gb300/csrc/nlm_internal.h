@@ -56,4 +56,7 @@ cudaError_t encode_tensor_map(CUtensorMap* map, bool fp16, int rank, const uint6
 // Address of the calling device's error word (see nlm_device_status).
 unsigned int* device_error_word();
 
+// Records `msg` as the calling thread's nlm_last_error() text; returns `code`.
+int report_error(int code, const char* msg);
+
 }  // namespace gnlm

@@ -63,6 +63,7 @@ def lib():
     L.nlm3d_workspace_bytes.restype = sz
     L.nlm3d_forward.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp, sz, vp]
     L.nlm3d_forward_host.argtypes = [vp, i, i, i, i, i, i, f, vp, u]
+    L.nlm3d_forward_noalloc.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp]
     L.nlm3d_stage.argtypes = [vp, i, i, i, i, i, i, f, u, vp, sz, vp]
     L.nlm3d_forward_staged.argtypes = [vp, sz, i, i, i, i, i, f, vp, vp, u, vp]
     L.nlm2d_workspace_bytes.argtypes = [i, i, i, i, u]

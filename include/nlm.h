@@ -108,6 +108,24 @@ int nlm3d_forward_staged(const void* d_ws, size_t ws_bytes, int X, int Y, int Z,
                          nlm_stream_t stream);
 
 /*
+ * Allocation-free form of nlm3d_forward (no counterpart in the reference).  For
+ * callers that must not allocate device memory while they run: plug-ins whose host
+ * application owns all GPU memory through its own pool, and fixed-budget real-time
+ * pipelines that reserve everything at start-up, where a cudaMalloc can fail
+ * mid-run and a cudaFree stalls the whole device.  The staging scratch is a 16 MiB
+ * array compiled into libgnlm.so, held on every GPU that loads the library until
+ * the process exits.  Volumes whose staged copy needs more (sr 3, pr 1: beyond 152^3
+ * in FP32, 192^3 with NLM_FLAG_FP16_STORAGE) return NLM_ERR_WORKSPACE.  The first
+ * call on each device looks up the array's device address (make that first call
+ * before any stream capture).  All calls on a device share the array: calls whose
+ * GPU work overlaps race, so serialise them (e.g. on one stream).  The array keeps
+ * the last call's contents; nothing in it needs to start at zero.
+ */
+int nlm3d_forward_noalloc(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
+                          float h, float* d_out, float* d_zsum, unsigned int flags,
+                          nlm_stream_t stream);
+
+/*
  * Host-buffer form with the reference's calling semantics: synchronous, host
  * pointers in and out, device memory owned by the library (cached per device).
  * The host->device copy, the kernels and the device->host copy run in order on a
