@@ -1,0 +1,58 @@
+#!/bin/bash
+# Builds the reference's own generic NLM kernels as sm_103a cubins into oracle/_ref/,
+# from the sources where they lie (no copies): each configuration gets a directory of
+# symlinks to the reference's main.cu / main.h / cuda_utility.h next to a config.h with
+# that configuration's values, which is how the reference itself is configured
+# (3DNLM/run.sh:13-19 rewrites config.h).  Only device code is built (-cubin); the
+# cubins are test infrastructure, loaded by tests/golden/make_ref_golden.py.
+#
+# At NS=3 the reference's host launcher names shift kernels that exist only for
+# NS=5..17 (3DNLM/main.cu:7644-7666 vs the #if NS== blocks); -D aliases point those
+# names at the generic kernel so the file compiles; only the generic kernel is launched.
+set -euo pipefail
+REF=${REF:-/root/reference}
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+NVCC=${NVCC:-nvcc}
+ARCH="-arch=sm_103a"
+[ -d "$REF/3DNLM" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
+mkdir -p "$OUT"
+
+build3d() {  # SS NS X Y DEPTH
+    local ss=$1 ns=$2 x=$3 y=$4 d=$5
+    local name="ref3d_ss${ss}_ns${ns}_x${x}_y${y}_d${d}"
+    local dir="$OUT/src_$name"
+    mkdir -p "$dir"
+    for f in main.cu main.h cuda_utility.h; do ln -sf "$REF/3DNLM/$f" "$dir/$f"; done
+    cat > "$dir/config.h" <<CFG
+#ifndef CONFIG_H
+#define CONFIG_H
+#define SS $ss
+#define NS $ns
+#define IMAGE_SIZE_X $x
+#define IMAGE_SIZE_Y $y
+#define depth $d
+#endif
+CFG
+    local alias=""
+    if [ "$ns" -lt 5 ]; then
+        alias="-DNLmeansOnGPU_shift_1=shuffle_without_optimization -DNLmeansOnGPU_shift_2=shuffle_without_optimization -DNLmeansOnGPU_shift_3=shuffle_without_optimization"
+    fi
+    $NVCC $ARCH -O3 -cubin $alias -I"$dir" -o "$OUT/$name.cubin" "$dir/main.cu"
+    echo "$OUT/$name.cubin"
+}
+
+build2d() {
+    local dir="$OUT/src_ref2d"
+    mkdir -p "$dir"
+    for f in main.cu main.h cuda_utility.h; do ln -sf "$REF/2D NLM/11x11/$f" "$dir/$f"; done
+    $NVCC $ARCH -O3 -cubin -I"$dir" -o "$OUT/ref2d.cubin" "$dir/main.cu"
+    echo "$OUT/ref2d.cubin"
+}
+
+# Reads stay inside the padded buffers for these sizes: X a multiple of 33-NS,
+# Y a multiple of 64 (16 blocks x 4 rows; Y = 128 exercises the y slide), depth a
+# multiple of 8; 2D: X = Y a multiple of both 22 and 64.
+build3d 7 3 120 128 16
+build3d 7 5 112 128 16
+build2d
