@@ -55,6 +55,13 @@ std::map<int, HostPath*> g_host;
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
+// Autotuned tile-shape variant per (dims, sr, pr, fp16); absent = variant 0.
+std::map<long long, int> g_tuned;
+long long tune_key(int dims, int sr, int pr, bool fp16) {
+    return ((long long)dims << 40) | ((long long)(sr & 0xffff) << 24) | ((long long)(pr & 0xffff) << 8) |
+           (fp16 ? 1 : 0);
+}
+
 bool valid_dtype(int d) { return d == NLM_U8 || d == NLM_F16 || d == NLM_F32; }
 size_t dtype_bytes(int d) { return d == NLM_U8 ? 1 : (d == NLM_F16 ? 2 : 4); }
 
@@ -136,6 +143,12 @@ int check_dims3(int X, int Y, int Z, int H) {
 }  // namespace
 
 int report_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+int tuned_variant(int dims, int sr, int pr, bool fp16) {
+    std::lock_guard<std::mutex> lk(g_mutex);
+    auto it = g_tuned.find(tune_key(dims, sr, pr, fp16));
+    return it == g_tuned.end() ? 0 : it->second;
+}
 
 unsigned int* device_error_word() {
     int dev = 0;
@@ -261,8 +274,9 @@ static int fwd3d_staged_impl(const void* d_ws, int X, int Y, int Z, int sr, int 
     const int H = sr + pr;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
     Staging st = make_staging(X, Y, Z, H, H, fp16);
-    cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, 1.0f / weight_scale(pr, 3, h), d_out,
-                                     d_zsum, device_error_word(), stream);
+    cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, tuned_variant(3, sr, pr, fp16),
+                                     1.0f / weight_scale(pr, 3, h), d_out, d_zsum,
+                                     device_error_word(), stream);
     if (e != cudaSuccess) return cuda_fail(e, "nlm3d_fwd launch");
     return NLM_OK;
 }
@@ -330,6 +344,88 @@ int nlm2d_forward(const void* d_in, int in_dtype, int X, int Y, int sr, int pr, 
     e = launch_nlm2d_fwd(st, d_ws, sr, pr, fp16, 1.0f / s, d_out, d_zsum, ew, stream);
     if (e != cudaSuccess) return cuda_fail(e, "nlm2d_fwd launch");
     return NLM_OK;
+}
+
+int nlm_variant_count(int dims, unsigned int flags) {
+    if (dims == 3) return nlm3d_fwd_variant_count((flags & NLM_FLAG_FP16_STORAGE) != 0);
+    if (dims == 2) return 1;
+    return fail(NLM_ERR_INVALID_ARG, "dims must be 2 or 3");
+}
+
+int nlm_set_variant(int dims, int sr, int pr, unsigned int flags, int variant) {
+    const int n = nlm_variant_count(dims, flags);
+    if (n < 0) return n;
+    if (variant < -1 || variant >= n)
+        return fail(NLM_ERR_INVALID_ARG, "variant %d outside [-1, %d)", variant, n);
+    std::lock_guard<std::mutex> lk(g_mutex);
+    const long long k = tune_key(dims, sr, pr, (flags & NLM_FLAG_FP16_STORAGE) != 0);
+    if (variant < 0)
+        g_tuned.erase(k);
+    else
+        g_tuned[k] = variant;
+    return NLM_OK;
+}
+
+int nlm_get_variant(int dims, int sr, int pr, unsigned int flags) {
+    if (dims != 2 && dims != 3) return fail(NLM_ERR_INVALID_ARG, "dims must be 2 or 3");
+    return tuned_variant(dims, sr, pr, (flags & NLM_FLAG_FP16_STORAGE) != 0);
+}
+
+int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int flags,
+                 float* times_ms, nlm_stream_t stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (dims != 3) {
+        if (dims == 2) return 0;  // one 2D variant
+        return fail(NLM_ERR_INVALID_ARG, "dims must be 2 or 3");
+    }
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    int rc = check_dims3(X, Y, Z, sr + pr);
+    if (rc) return rc;
+    if (!nlm3d_fwd_supported(sr, pr, fp16))
+        return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
+    const Staging st = make_staging(X, Y, Z, sr + pr, sr + pr, fp16);
+    const size_t nvox = (size_t)X * Y * Z;
+    void *d_in = nullptr, *d_ws = nullptr;
+    float* d_out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int best = -1;
+    float best_ms = 0.f;
+    const int nv = nlm3d_fwd_variant_count(fp16);
+    cudaError_t e = cudaMalloc(&d_in, nvox * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, nvox * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_ws, st.bytes());
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_in, 0, nvox * sizeof(float), stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const float s = weight_scale(pr, 3, 0.05f);
+    if (e == cudaSuccess) e = launch_stage(d_in, NLM_F32, false, s, st, d_ws, stream);
+    for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+        float ms = 1e30f;
+        for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+            e = cudaEventRecord(e0, stream);
+            if (e == cudaSuccess)
+                e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, v, 1.0f / s, d_out, nullptr,
+                                     device_error_word(), stream);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float t = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+            if (rep > 0 && t < ms) ms = t;  // first run is a warm-up
+        }
+        if (times_ms) times_ms[v] = ms;
+        if (e == cudaSuccess && (best < 0 || ms < best_ms)) {
+            best = v;
+            best_ms = ms;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d_in);
+    cudaFree(d_out);
+    cudaFree(d_ws);
+    if (e != cudaSuccess) return cuda_fail(e, "nlm_autotune");
+    nlm_set_variant(3, sr, pr, flags, best);
+    return best;
 }
 
 static HostPath* host_path(int dev) {

@@ -37,9 +37,14 @@ cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float sca
 // 3D forward over a staged volume.  Returns cudaErrorNotSupported when the
 // (sr, pr, fp16) combination has no compiled instance.
 cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
-                             float inv_scale, float* out, float* zsum, unsigned int* errword,
-                             cudaStream_t stream);
+                             int variant, float inv_scale, float* out, float* zsum,
+                             unsigned int* errword, cudaStream_t stream);
 bool nlm3d_fwd_supported(int sr, int pr, bool fp16);
+int nlm3d_fwd_variant_count(bool fp16);
+
+// Tile-shape variant the forward uses for (dims, sr, pr, fp16): the autotuned
+// choice if one was recorded, else 0.
+int tuned_variant(int dims, int sr, int pr, bool fp16);
 
 // 2D forward over a staged image (Z = 1, Hz = 0).
 cudaError_t launch_nlm2d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,

@@ -63,6 +63,10 @@ def lib():
     L.nlm3d_workspace_bytes.restype = sz
     L.nlm3d_forward.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp, sz, vp]
     L.nlm3d_forward_host.argtypes = [vp, i, i, i, i, i, i, f, vp, u]
+    L.nlm_variant_count.argtypes = [i, u]
+    L.nlm_set_variant.argtypes = [i, i, i, u, i]
+    L.nlm_get_variant.argtypes = [i, i, i, u]
+    L.nlm_autotune.argtypes = [i, i, i, i, i, i, u, ctypes.POINTER(ctypes.c_float), vp]
     L.nlm3d_forward_noalloc.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp]
     L.nlm3d_stage.argtypes = [vp, i, i, i, i, i, i, f, u, vp, sz, vp]
     L.nlm3d_forward_staged.argtypes = [vp, sz, i, i, i, i, i, f, vp, vp, u, vp]
@@ -80,6 +84,12 @@ def last_error():
 
 def check(rc):
     if rc != NLM_OK:
+        raise NLMError(rc, last_error())
+    return rc
+
+
+def check_nonneg(rc):
+    if rc < 0:
         raise NLMError(rc, last_error())
     return rc
 
@@ -160,6 +170,30 @@ def nlm3d_forward_staged(workspace, shape, sr, pr, h, out, zsum=None, fp16_stora
                                      X, Y, Z, sr, pr, float(h), _ptr(out), _ptr(zsum), flags,
                                      _stream_ptr(stream)))
     return out
+
+
+def variant_count(dims, fp16_storage=False):
+    return check_nonneg(lib().nlm_variant_count(dims, NLM_FLAG_FP16_STORAGE if fp16_storage else 0))
+
+
+def set_variant(dims, sr, pr, variant, fp16_storage=False):
+    check(lib().nlm_set_variant(dims, sr, pr, NLM_FLAG_FP16_STORAGE if fp16_storage else 0,
+                                int(variant)))
+
+
+def get_variant(dims, sr, pr, fp16_storage=False):
+    return check_nonneg(lib().nlm_get_variant(dims, sr, pr,
+                                              NLM_FLAG_FP16_STORAGE if fp16_storage else 0))
+
+
+def autotune(dims, shape, sr, pr, fp16_storage=False, stream=None):
+    """Time every tile-shape variant; returns (best_index, times_ms list)."""
+    flags = NLM_FLAG_FP16_STORAGE if fp16_storage else 0
+    n = variant_count(dims, fp16_storage)
+    times = (ctypes.c_float * n)()
+    Z, Y, X = shape if len(shape) == 3 else (1,) + tuple(shape)
+    best = check_nonneg(lib().nlm_autotune(dims, X, Y, Z, sr, pr, flags, times, _stream_ptr(stream)))
+    return best, list(times)
 
 
 def nlm2d_forward(x, sr, pr, h, fp16_storage=False, prepadded=False, return_zsum=False,

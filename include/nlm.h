@@ -135,6 +135,26 @@ int nlm3d_forward_noalloc(const void* d_in, int in_dtype, int X, int Y, int Z, i
 int nlm3d_forward_host(const void* h_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
                        float h, float* h_out, unsigned int flags);
 
+/* ------------------------------------------------------------ autotuner -- */
+
+/*
+ * Tile-shape variants of the fused kernels (no counterpart in the reference,
+ * whose block/grid shape is fixed by macros, 3DNLM/main.cu:15-21).  Forward calls
+ * use the recorded variant for (dims, sr, pr, FP16 flag), or variant 0.
+ */
+int nlm_variant_count(int dims, unsigned int flags);
+int nlm_set_variant(int dims, int sr, int pr, unsigned int flags, int variant); /* -1 = reset */
+int nlm_get_variant(int dims, int sr, int pr, unsigned int flags);
+
+/*
+ * Times every variant for (dims, sr, pr, flags) on an X x Y x Z volume (temporary
+ * buffers allocated here; synchronises `stream`), records the fastest and returns
+ * its index (>= 0) or a negative status.  times_ms (nullable) receives
+ * nlm_variant_count() per-variant best-of-3 times in milliseconds.
+ */
+int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int flags,
+                 float* times_ms, nlm_stream_t stream);
+
 /* ---------------------------------------------------------------- 2D ------ */
 
 size_t nlm2d_workspace_bytes(int X, int Y, int sr, int pr, unsigned int flags);

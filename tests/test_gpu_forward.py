@@ -196,3 +196,32 @@ def test_legacy_driver_binary(torch_cuda, gnlm_lib, tmp_path):
 
 def test_device_status_clean(torch_cuda, gnlm_lib):
     assert gnlm_lib.device_status() == (0, 0)
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+def test_3d_every_tile_variant(torch_cuda, gnlm_lib, fp16):
+    """Each autotuner variant (tile shape, register/shared reference values, Kahan
+    sums for FP16 storage) against the FP64 oracle, on sizes with ragged edges."""
+    tol = TOL_F16 if fp16 else TOL_F32
+    cases = [((13, 37, 67), 3, 1), ((9, 20, 95), 5, 1), ((11, 23, 41), 3, 2)]
+    for shape, sr, pr in cases:
+        v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=5, sigma=0.05, seed=sum(shape) + sr,
+                                         radii=(2.0, 8.0))
+        o = O.nlm3d(v, sr, pr, 0.05, dtype=np.float64)
+        try:
+            for var in range(gnlm_lib.variant_count(3, fp16)):
+                gnlm_lib.set_variant(3, sr, pr, var, fp16)
+                g = _gpu3d(torch_cuda, gnlm_lib, v, sr, pr, 0.05, fp16_storage=fp16)
+                assert np.abs(g - o).max() <= tol, (shape, sr, pr, var)
+        finally:
+            gnlm_lib.set_variant(3, sr, pr, -1, fp16)
+    assert gnlm_lib.device_status() == (0, 0)
+
+
+def test_autotune_records_a_variant(torch_cuda, gnlm_lib):
+    best, times = gnlm_lib.autotune(3, (32, 64, 90), 3, 1)
+    assert 0 <= best < len(times) and all(t > 0 for t in times)
+    assert gnlm_lib.get_variant(3, 3, 1) == best
+    assert times[best] == min(times)
+    gnlm_lib.set_variant(3, 3, 1, -1)
+    assert gnlm_lib.get_variant(3, 3, 1) == 0
