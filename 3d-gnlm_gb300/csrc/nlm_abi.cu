@@ -346,6 +346,41 @@ int nlm2d_forward(const void* d_in, int in_dtype, int X, int Y, int sr, int pr, 
     return NLM_OK;
 }
 
+size_t nlm3d_adjoint_workspace_bytes(int X, int Y, int Z, int sr, int pr) {
+    if (X < 1 || Y < 1 || Z < 1 || sr < 0 || pr < 0 || !nlm3d_adj_supported(sr, pr)) return 0;
+    const Staging st = make_staging(X, Y, Z, sr + pr, sr + pr, false);
+    return 4 * st.bytes() + align_up(adj3d_ctas(st, sr, pr) * sizeof(double), kAlign);
+}
+
+int nlm3d_adjoint(const float* d_in, const float* d_out, const float* d_zsum, const float* d_gout,
+                  int X, int Y, int Z, int sr, int pr, float h, float* d_gin, double* d_hgrad,
+                  void* d_ws, size_t ws_bytes, nlm_stream_t stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    int rc = check_common(d_in, d_gin, NLM_F32, sr, pr, h, 0);
+    if (rc) return rc;
+    if (!d_out || !d_zsum || !d_gout)
+        return fail(NLM_ERR_INVALID_ARG, "adjoint needs out, zsum and the upstream gradient");
+    if ((rc = check_dims3(X, Y, Z, sr + pr))) return rc;
+    if (!nlm3d_adj_supported(sr, pr))
+        return fail(NLM_ERR_UNSUPPORTED, "3D adjoint (sr=%d, pr=%d) not compiled in", sr, pr);
+    const Staging st = make_staging(X, Y, Z, sr + pr, sr + pr, false);
+    if ((rc = resolve_ws(&d_ws, &ws_bytes, nlm3d_adjoint_workspace_bytes(X, Y, Z, sr, pr), stream)))
+        return rc;
+    char* base = static_cast<char*>(d_ws);
+    void* staged = base;
+    float* G = reinterpret_cast<float*>(base + st.bytes());
+    float* O = reinterpret_cast<float*>(base + 2 * st.bytes());
+    float* gpad = reinterpret_cast<float*>(base + 3 * st.bytes());
+    double* hpart = reinterpret_cast<double*>(base + 4 * st.bytes());
+    const float s = weight_scale(pr, 3, h);
+    cudaError_t e = launch_stage(d_in, NLM_F32, false, s, st, staged, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint staging");
+    e = launch_nlm3d_adj(st, staged, d_out, d_zsum, d_gout, sr, pr, s, h, d_gin, d_hgrad, G, O,
+                         gpad, hpart, device_error_word(), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nlm3d_adjoint launch");
+    return NLM_OK;
+}
+
 int nlm_variant_count(int dims, unsigned int flags) {
     if (dims == 3) return nlm3d_fwd_variant_count((flags & NLM_FLAG_FP16_STORAGE) != 0);
     if (dims == 2) return 1;

@@ -42,6 +42,15 @@ cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int 
 bool nlm3d_fwd_supported(int sr, int pr, bool fp16);
 int nlm3d_fwd_variant_count(bool fp16);
 
+// 3D adjoint (see nlm3d_adj.cu).  Scratch: G, out', gpad' (each st.bytes()) and
+// adj3d_ctas() doubles of h partial sums.
+bool nlm3d_adj_supported(int sr, int pr);
+size_t adj3d_ctas(const Staging& st, int sr, int pr);
+cudaError_t launch_nlm3d_adj(const Staging& st, const void* staged, const float* d_out,
+                             const float* d_zsum, const float* d_gout, int sr, int pr, float s,
+                             float h, float* gin, double* hgrad, float* G, float* O, float* gpad,
+                             double* hpart, unsigned int* errword, cudaStream_t stream);
+
 // Tile-shape variant the forward uses for (dims, sr, pr, fp16): the autotuned
 // choice if one was recorded, else 0.
 int tuned_variant(int dims, int sr, int pr, bool fp16);

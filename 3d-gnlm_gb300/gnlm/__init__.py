@@ -63,6 +63,9 @@ def lib():
     L.nlm3d_workspace_bytes.restype = sz
     L.nlm3d_forward.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp, sz, vp]
     L.nlm3d_forward_host.argtypes = [vp, i, i, i, i, i, i, f, vp, u]
+    L.nlm3d_adjoint_workspace_bytes.argtypes = [i, i, i, i, i]
+    L.nlm3d_adjoint_workspace_bytes.restype = sz
+    L.nlm3d_adjoint.argtypes = [vp, vp, vp, vp, i, i, i, i, i, f, vp, vp, vp, sz, vp]
     L.nlm_variant_count.argtypes = [i, u]
     L.nlm_set_variant.argtypes = [i, i, i, u, i]
     L.nlm_get_variant.argtypes = [i, i, i, u]
@@ -170,6 +173,24 @@ def nlm3d_forward_staged(workspace, shape, sr, pr, h, out, zsum=None, fp16_stora
                                      X, Y, Z, sr, pr, float(h), _ptr(out), _ptr(zsum), flags,
                                      _stream_ptr(stream)))
     return out
+
+
+def nlm3d_adjoint(x, out, zsum, gout, sr, pr, h, gin=None, hgrad=None, workspace=None,
+                  stream=None):
+    """dL/dv (float32 [Z, Y, X]) and dL/dh (float64 CUDA scalar) of the 3D forward."""
+    torch = _torch()
+    Z, Y, X = x.shape
+    if gin is None:
+        gin = torch.empty_like(x)
+    if hgrad is None:
+        hgrad = torch.zeros(1, dtype=torch.float64, device=x.device)
+    ws_ptr, ws_bytes = None, 0
+    if workspace is not None:
+        ws_ptr, ws_bytes = ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+    check(lib().nlm3d_adjoint(_ptr(x), _ptr(out), _ptr(zsum), _ptr(gout), X, Y, Z, sr, pr,
+                              float(h), _ptr(gin), _ptr(hgrad), ws_ptr, ws_bytes,
+                              _stream_ptr(stream)))
+    return gin, hgrad
 
 
 def variant_count(dims, fp16_storage=False):

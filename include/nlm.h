@@ -135,6 +135,20 @@ int nlm3d_forward_noalloc(const void* d_in, int in_dtype, int X, int Y, int Z, i
 int nlm3d_forward_host(const void* h_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
                        float h, float* h_out, unsigned int flags);
 
+/*
+ * Adjoint of nlm3d_forward (no counterpart in the reference): for an upstream
+ * gradient d_gout = dL/dout it writes dL/dv into d_gin (X*Y*Z floats) and, if
+ * d_hgrad is not NULL, dL/dh into the one device double d_hgrad.  Takes the
+ * forward's input d_in (FP32), output d_out and weight sums d_zsum.  The
+ * per-offset weights are recomputed, not stored; gradients that land on padding
+ * voxels are folded back onto their REFLECT_101 sources; every output is a
+ * gather and dL/dh a fixed-order sum, so results are bitwise reproducible.
+ */
+size_t nlm3d_adjoint_workspace_bytes(int X, int Y, int Z, int sr, int pr);
+int nlm3d_adjoint(const float* d_in, const float* d_out, const float* d_zsum, const float* d_gout,
+                  int X, int Y, int Z, int sr, int pr, float h, float* d_gin, double* d_hgrad,
+                  void* d_ws, size_t ws_bytes, nlm_stream_t stream);
+
 /* ------------------------------------------------------------ autotuner -- */
 
 /*

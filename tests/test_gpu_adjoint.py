@@ -1,0 +1,124 @@
+"""GPU tests of the 3D adjoint (nlm3d_adjoint) through the C ABI.
+
+* against the FP64 oracle adjoint (direct form), which is itself checked against
+  FP64 central differences in test_oracle.py;
+* bitwise determinism (gather form, fixed-order h reduction);
+* a torch.autograd.Function harness (forward and backward both the CUDA kernels)
+  checked against FP64 central differences of the FP64 oracle forward, on random
+  voxels and on h;
+* a few gradient-descent steps on h that lower the error to the clean phantom.
+FP32 kernels against FP64 references: bar 2e-4 of the gradient's scale.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from gnlm import phantom
+
+pytestmark = pytest.mark.gpu
+
+REL = 2e-4
+
+
+def _run(torch, gnlm, v, sr, pr, h, g):
+    x = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float32)).cuda()
+    out, zs = gnlm.nlm3d_forward(x, sr, pr, h, return_zsum=True)
+    gin, hg = gnlm.nlm3d_adjoint(x, out, zs, torch.from_numpy(g.astype(np.float32)).cuda(), sr, pr, h)
+    torch.cuda.synchronize()
+    return gin.cpu().numpy(), float(hg.item()), out.cpu().numpy()
+
+
+@pytest.mark.parametrize("shape,sr,pr", [((8, 10, 12), 2, 1), ((12, 13, 14), 3, 1),
+                                         ((9, 11, 40), 1, 1), ((10, 12, 12), 3, 2),
+                                         ((7, 9, 11), 5, 1), ((3, 4, 5), 3, 1)])
+def test_adjoint_matches_fp64_oracle(torch_cuda, gnlm_lib, shape, sr, pr):
+    v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=4, sigma=0.05, seed=sum(shape) + sr,
+                                     radii=(1.5, 6.0))
+    h = 0.06
+    g = np.random.default_rng(sr * 7 + pr).standard_normal(shape)
+    gin, hg, out = _run(torch_cuda, gnlm_lib, v, sr, pr, h, g)
+    rgin, rhg, rout = O.nlm3d_adjoint(v.astype(np.float64), sr, pr, h, g)
+    assert np.abs(out - rout).max() <= 1e-5
+    scale = np.abs(rgin).max()
+    assert np.abs(gin - rgin).max() <= REL * scale, (np.abs(gin - rgin).max(), scale)
+    assert abs(hg - rhg) <= REL * max(abs(rhg), 1.0), (hg, rhg)
+    assert gnlm_lib.device_status() == (0, 0)
+
+
+def test_adjoint_is_deterministic(torch_cuda, gnlm_lib):
+    v, _ = phantom.ellipsoid_phantom((20, 24, 60), sigma=0.05, seed=5)
+    g = np.random.default_rng(1).standard_normal(v.shape)
+    a = _run(torch_cuda, gnlm_lib, v, 3, 1, 0.05, g)
+    b = _run(torch_cuda, gnlm_lib, v, 3, 1, 0.05, g)
+    assert np.array_equal(a[0], b[0]) and a[1] == b[1]
+
+
+class NLMFunction:
+    """torch.autograd.Function over the CUDA forward and adjoint (test harness only)."""
+
+    @staticmethod
+    def make(torch, gnlm, sr, pr):
+        class _F(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, x, h):
+                out, zs = gnlm.nlm3d_forward(x.detach().contiguous(), sr, pr, float(h))
+                ctx.save_for_backward(x, out, zs, h)
+                return out
+
+            @staticmethod
+            def backward(ctx, gout):
+                x, out, zs, h = ctx.saved_tensors
+                gin, hg = gnlm.nlm3d_adjoint(x.contiguous(), out, zs, gout.contiguous(), sr, pr,
+                                             float(h))
+                return gin, hg.to(h.dtype).reshape(h.shape)
+
+        return _F.apply
+
+
+def test_autograd_harness_against_fp64_finite_differences(torch_cuda, gnlm_lib):
+    torch = torch_cuda
+    sr, pr, h0 = 2, 1, 0.07
+    v, _ = phantom.ellipsoid_phantom((8, 9, 10), n_ellipsoids=3, sigma=0.05, seed=9, radii=(2.0, 5.0))
+    g = np.random.default_rng(2).standard_normal(v.shape)
+    f = NLMFunction.make(torch, gnlm_lib, sr, pr)
+    x = torch.from_numpy(v).cuda().requires_grad_(True)
+    h = torch.tensor([h0], dtype=torch.float64, device="cuda", requires_grad=True)
+    out = f(x, h)
+    (out * torch.from_numpy(g.astype(np.float32)).cuda()).sum().backward()
+    gx = x.grad.cpu().numpy()
+    gh = float(h.grad.item())
+    v64 = v.astype(np.float64)
+
+    def L(vv, hh):
+        return float((O.nlm3d(vv, sr, pr, hh, dtype=np.float64, form=O.FORM_DIRECT) * g).sum())
+
+    eps = 1e-6
+    rng = np.random.default_rng(3)
+    scale = np.abs(gx).max()
+    for _ in range(8):
+        idx = tuple(int(rng.integers(0, s)) for s in v.shape)
+        vp, vm = v64.copy(), v64.copy()
+        vp[idx] += eps
+        vm[idx] -= eps
+        fd = (L(vp, h0) - L(vm, h0)) / (2 * eps)
+        assert abs(gx[idx] - fd) <= REL * scale, (idx, gx[idx], fd)
+    fdh = (L(v64, h0 + eps) - L(v64, h0 - eps)) / (2 * eps)
+    assert abs(gh - fdh) <= REL * max(1.0, abs(fdh)), (gh, fdh)
+
+
+def test_h_fit_by_gradient_descent_lowers_error(torch_cuda, gnlm_lib):
+    """Fit h against the clean phantom with the adjoint's dL/dh (L = MSE)."""
+    torch = torch_cuda
+    noisy, clean = phantom.ellipsoid_phantom((24, 32, 40), n_ellipsoids=6, sigma=0.05, seed=11)
+    x = torch.from_numpy(noisy).cuda()
+    c = torch.from_numpy(clean).cuda()
+    h = 0.02
+    losses = []
+    for _ in range(8):
+        out, zs = gnlm_lib.nlm3d_forward(x, 3, 1, h, return_zsum=True)
+        diff = out - c
+        losses.append(float((diff * diff).mean()))
+        gout = 2.0 * diff / diff.numel()
+        _, hg = gnlm_lib.nlm3d_adjoint(x, out, zs, gout, 3, 1, h)
+        h = max(1e-3, h - 0.02 / max(1e-12, abs(float(hg.item()))) * float(hg.item()) * 0.2)
+    assert losses[-1] < losses[0]
