@@ -38,6 +38,7 @@ struct Fwd2d {
     static constexpr int K = 2 * N + 1;
     static constexpr int ROWS = RY + 2 * N;
     static_assert(BX <= 256 && BY <= 256, "TMA box dimension > 256");
+    static_assert(BAR_OFF % 128 == 0, "the tile (at offset 0) and barrier stay 128-byte aligned");
 };
 
 template <int M, int N, typename T, int RY, int NW, int MINB>

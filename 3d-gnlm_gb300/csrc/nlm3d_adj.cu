@@ -37,8 +37,12 @@ struct Adj3d {
     static constexpr int BZ = RZ + 2 * HE;
     static constexpr int PLANE = BX * BY;
     static constexpr int FIELD_BYTES = BX * BY * BZ * 4;
-    static constexpr int BAR_OFF = 3 * FIELD_BYTES;
-    static constexpr int SMEM_BYTES = BAR_OFF + 128;
+    // each field starts on a 128-byte boundary: TMA tensor-copy destinations must
+    static constexpr int FIELD_STRIDE = adj_round(FIELD_BYTES, 128);
+    static constexpr int BAR_OFF = 3 * FIELD_STRIDE;          // mbarrier
+    static constexpr int RED_OFF = BAR_OFF + 128;             // per-warp h partials
+    static constexpr int SMEM_BYTES = RED_OFF + 32 * 8;
+    static_assert(FIELD_STRIDE % 128 == 0 && BAR_OFF % 128 == 0, "TMA destination alignment");
     static constexpr int K = 2 * N + 1;
     static constexpr int RT = RY + 4 * N, PT = RZ + 4 * N;  // difference window
     static constexpr int RD = RY + 2 * N, PD = RZ + 2 * N;  // distance window
@@ -82,10 +86,10 @@ __global__ void __launch_bounds__(32 * NW, 1)
     constexpr float kLn2 = 0.69314718055994531f;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* vt = reinterpret_cast<float*>(smem_raw);
-    float* gt = vt + C::FIELD_BYTES / 4;
-    float* ot = gt + C::FIELD_BYTES / 4;
+    float* gt = reinterpret_cast<float*>(smem_raw + C::FIELD_STRIDE);
+    float* ot = reinterpret_cast<float*>(smem_raw + 2 * C::FIELD_STRIDE);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF);
-    __shared__ double red[32];
+    double* red = reinterpret_cast<double*>(smem_raw + C::RED_OFF);
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;

@@ -51,6 +51,7 @@ struct Fwd3d {
     static constexpr int ROWS = RY + 2 * N;             // rows a thread sums
     static constexpr int PLANES = RZ + 2 * N;           // planes a thread streams
     static_assert(BX <= 256 && BY <= 256 && BZ <= 256, "TMA box dimension > 256");
+    static_assert(BAR_OFF % 128 == 0, "the tile (at offset 0) and barrier stay 128-byte aligned");
     static_assert(TILE_BYTES + 256 <= 227 * 1024, "tile exceeds shared memory");
 };
 

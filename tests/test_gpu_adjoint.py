@@ -61,7 +61,8 @@ class NLMFunction:
         class _F(torch.autograd.Function):
             @staticmethod
             def forward(ctx, x, h):
-                out, zs = gnlm.nlm3d_forward(x.detach().contiguous(), sr, pr, float(h))
+                out, zs = gnlm.nlm3d_forward(x.detach().contiguous(), sr, pr, float(h),
+                                             return_zsum=True)
                 ctx.save_for_backward(x, out, zs, h)
                 return out
 
@@ -120,5 +121,5 @@ def test_h_fit_by_gradient_descent_lowers_error(torch_cuda, gnlm_lib):
         losses.append(float((diff * diff).mean()))
         gout = 2.0 * diff / diff.numel()
         _, hg = gnlm_lib.nlm3d_adjoint(x, out, zs, gout, 3, 1, h)
-        h = max(1e-3, h - 0.02 / max(1e-12, abs(float(hg.item()))) * float(hg.item()) * 0.2)
+        h = max(1e-3, h - 0.004 * float(np.sign(hg.item())))  # normalised step
     assert losses[-1] < losses[0]
