@@ -1,0 +1,248 @@
+// The per-tile body of the fused 3D NLM forward, shared by the single-volume
+// kernel (nlm3d_fwd.cu) and the persistent batched kernel (nlm3d_batch.cu).
+//
+// Work decomposition (one output tile of XO x TY x RZ voxels):
+//   * The tile plus its halo (H = sr + pr voxels on each side) is loaded from
+//     the staged volume into shared memory by one TMA box copy
+//     (cp.async.bulk.tensor.3d) completing on an mbarrier.
+//   * Warp w owns RY output rows, lane l owns output column X0 + l - pr; lanes
+//     0..pr-1 and 32-pr..31 only feed the x box sum (the reference's
+//     33-NS outputs per warp, 3DNLM/main.cu:30).  Each thread owns an RY x RZ
+//     brick of voxels and keeps their weighted sums in registers across all
+//     (2sr+1)^3 search offsets.
+//   * Per offset: squared differences t^2 of (reference, candidate) values are
+//     summed along z with a register sliding window (add the entering plane,
+//     subtract the leaving one), along y from those row sums, and along x with
+//     warp shuffles (3DNLM/main.cu:58-103 sums x by shuffles and z by planes;
+//     its y cache in global memory, 3DNLM/main.cu:107,132-209, becomes
+//     on-chip register reuse here).
+//   * Weight w = 2^(-D') with D' = D log2(e)/(P h^2): the staging pass
+//     pre-scaled the volume so D' is the sum of squares itself, and one MUFU
+//     ex2 gives exp(-(D/P)/h^2) (3DNLM/main.cu:108-109).  num += w v, Z += w
+//     (3DNLM/main.cu:110-111); out = num / Z (3DNLM/main.cu:125).
+//
+// Algorithmic work per (voxel, offset): 12 FP32 flops (diff, square, 2 box-sum
+// add/sub per axis, scale, weight-sum add, weighted-value FMA) + 1 exp.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "nlm_device.cuh"
+
+namespace gnlm {
+
+constexpr int cgcd(int a, int b) { return b == 0 ? a : cgcd(b, a % b); }
+constexpr int cround(int v, int a) { return (v + a - 1) / a * a; }
+
+template <int M, int N, typename T, int RY, int RZ, int NW>
+struct Fwd3d {
+    static constexpr int H = M + N;
+    static constexpr int XO = 32 - 2 * N;             // output columns per warp
+    static constexpr int A = 16 / (int)sizeof(T);      // elements per 16 bytes
+    static constexpr int RMAX = A - cgcd(XO, A);       // max misalignment of X0
+    static constexpr int BX = cround(32 + 2 * M + RMAX, A);
+    static constexpr int TY = NW * RY;
+    static constexpr int BY = TY + 2 * H;
+    static constexpr int BZ = RZ + 2 * H;
+    static constexpr int PLANE = BX * BY;
+    static constexpr int TILE_BYTES = BX * BY * BZ * (int)sizeof(T);
+    static constexpr int BAR_OFF = cround(TILE_BYTES, 128);
+    static constexpr int SMEM_BYTES = BAR_OFF + 128;  // + mbarrier
+    static constexpr int THREADS = 32 * NW;
+    static constexpr int K = 2 * N + 1;                 // patch width
+    static constexpr int ROWS = RY + 2 * N;             // rows a thread sums
+    static constexpr int PLANES = RZ + 2 * N;           // planes a thread streams
+    static_assert(BX <= 256 && BY <= 256 && BZ <= 256, "TMA box dimension > 256");
+    static_assert(BAR_OFF % 128 == 0, "the tile (at offset 0) and barrier stay 128-byte aligned");
+    static_assert(TILE_BYTES + 256 <= 227 * 1024, "tile exceeds shared memory");
+};
+
+// Compensated (Kahan) accumulation of a packed pair of running sums.
+struct Kahan2 {
+    float2 s, c;
+};
+__device__ __forceinline__ void kahan_add(Kahan2& k, float2 v) {
+    const float2 y = __fadd2_rn(v, make_float2(-k.c.x, -k.c.y));
+    const float2 t = __fadd2_rn(k.s, y);
+    k.c = __fadd2_rn(__fadd2_rn(t, make_float2(-k.s.x, -k.s.y)), make_float2(-y.x, -y.y));
+    k.s = t;
+}
+
+// AREG: the thread's reference values (its column, ROWS rows, PLANES planes) are
+// loaded into registers once; they are the same for every search offset.
+// KAHAN: Z and num are Kahan-compensated (precision form).
+// Rows are processed in pairs so that everything after the first difference runs
+// as packed FP32x2 arithmetic (FFMA2/FADD2): one issue slot per two operations.
+// One output tile (bx, by, bz) of a staged volume: thread 0 issues the TMA box
+// copy of tile + halo into `tile` (completing on `bar`), every thread waits for
+// phase `parity`, computes its brick over all offsets and stores.  Returns false
+// if the copy did not land within the wait limit (the error word is set).
+template <int M, int N, typename T, int RY, int RZ, int NW, bool AREG, bool KAHAN>
+__device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint64_t* bar,
+                                           uint32_t parity, int bx, int by, int bz, int X, int Y,
+                                           int Z, float inv_scale, float* __restrict__ out,
+                                           float* __restrict__ zsum, unsigned int* errword) {
+    using C = Fwd3d<M, N, T, RY, RZ, NW>;
+    static_assert(RY % 2 == 0, "rows are processed in pairs");
+    constexpr int RP = C::ROWS / 2;  // row pairs a thread sums
+    constexpr int OP = RY / 2;       // output row pairs
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int X0 = bx * C::XO;
+    const int Y0 = by * C::TY;
+    const int Z0 = bz * RZ;
+    const int xs = X0 & ~(C::A - 1);  // 16-byte aligned TMA start column
+    const int ral = X0 - xs;
+
+    if (threadIdx.x == 0) {
+        fence_proxy_async_smem();  // earlier generic reads of the tile before the async write
+        mbar_arrive_expect_tx(bar, C::TILE_BYTES);
+        tma_load_3d(tile, map, xs, Y0, Z0, bar);
+    }
+    if (!mbar_wait_bounded(bar, parity)) {
+        if (threadIdx.x == 0) {
+            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
+            mbar_wait_bounded(bar, parity);  // give an in-flight copy a last chance to land
+        }
+        return false;
+    }
+
+    // Reference values: lane's column, rows warp*RY + H - N + rr, planes H - N + pl.
+    const T* aptr = tile + (C::H - N) * C::PLANE + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
+
+    float2 areg[AREG ? C::PLANES : 1][AREG ? RP : 1];
+    if constexpr (AREG) {
+#pragma unroll
+        for (int pl = 0; pl < C::PLANES; ++pl)
+#pragma unroll
+            for (int rp = 0; rp < RP; ++rp)
+                areg[pl][rp] = make_float2(to_f32(aptr[pl * C::PLANE + (2 * rp) * C::BX]),
+                                           to_f32(aptr[pl * C::PLANE + (2 * rp + 1) * C::BX]));
+    }
+
+    // Accumulators for output row pairs (r, r+1) and planes q.
+    Kahan2 zacc[OP][RZ], nacc[OP][RZ];
+#pragma unroll
+    for (int r = 0; r < OP; ++r)
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) {
+            zacc[r][q].s = nacc[r][q].s = make_float2(0.f, 0.f);
+            zacc[r][q].c = nacc[r][q].c = make_float2(0.f, 0.f);
+        }
+    const float2 minus1 = make_float2(-1.f, -1.f);
+
+    for (int oz = -M; oz <= M; ++oz) {
+        for (int oy = -M; oy <= M; ++oy) {
+            for (int ox = -M; ox <= M; ++ox) {
+                const T* bptr = aptr + oz * C::PLANE + oy * C::BX + ox;
+                float2 S[RP];          // z-window sums of t^2, row pairs
+                float2 tr[C::K][RP];   // ring of the last K planes of t, row pairs
+                float cand[N + 1][RY]; // candidate centre values of the last N+1 planes
+#pragma unroll
+                for (int pl = 0; pl < C::PLANES; ++pl) {
+#pragma unroll
+                    for (int rp = 0; rp < RP; ++rp) {
+                        const float b0 = to_f32(bptr[pl * C::PLANE + (2 * rp) * C::BX]);
+                        const float b1 = to_f32(bptr[pl * C::PLANE + (2 * rp + 1) * C::BX]);
+                        float2 a2;
+                        if constexpr (AREG)
+                            a2 = areg[pl][rp];
+                        else
+                            a2 = make_float2(to_f32(aptr[pl * C::PLANE + (2 * rp) * C::BX]),
+                                             to_f32(aptr[pl * C::PLANE + (2 * rp + 1) * C::BX]));
+                        const float2 t = __ffma2_rn(make_float2(b0, b1), minus1, a2);  // a - b
+                        if (pl == 0)
+                            S[rp] = __fmul2_rn(t, t);
+                        else
+                            S[rp] = __ffma2_rn(t, t, S[rp]);
+                        if (pl >= C::K) {
+                            const float2 to = tr[(pl - C::K) % C::K][rp];
+                            S[rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S[rp]);
+                        }
+                        tr[pl % C::K][rp] = t;
+                        const int r0 = 2 * rp, r1 = 2 * rp + 1;
+                        if (r0 >= N && r0 < RY + N) cand[pl % (N + 1)][r0 - N] = b0;
+                        if (r1 >= N && r1 < RY + N) cand[pl % (N + 1)][r1 - N] = b1;
+                    }
+                    if (pl >= 2 * N) {
+                        const int q = pl - 2 * N;
+                        // y box over rows: Yv[r] = sum_{k<K} Srow[r+k]
+                        float Srow[C::ROWS];
+#pragma unroll
+                        for (int rp = 0; rp < RP; ++rp) {
+                            Srow[2 * rp] = S[rp].x;
+                            Srow[2 * rp + 1] = S[rp].y;
+                        }
+                        float Yv[RY];
+                        if constexpr (N == 1) {
+#pragma unroll
+                            for (int r = 0; r < RY; r += 2) {  // 3 adds per 2 outputs
+                                const float u = Srow[r + 1] + Srow[r + 2];
+                                Yv[r] = Srow[r] + u;
+                                Yv[r + 1] = u + Srow[r + 3];
+                            }
+                        } else {
+                            float acc = 0.f;
+#pragma unroll
+                            for (int k = 0; k < C::K; ++k) acc += Srow[k];
+                            Yv[0] = acc;
+#pragma unroll
+                            for (int r = 1; r < RY; ++r) {
+                                acc = acc + Srow[r + C::K - 1] - Srow[r - 1];
+                                Yv[r] = acc;
+                            }
+                        }
+#pragma unroll
+                        for (int op = 0; op < OP; ++op) {
+                            float2 xv = make_float2(Yv[2 * op], Yv[2 * op + 1]);
+#pragma unroll
+                            for (int k = 1; k <= N; ++k) {
+                                const float2 dn =
+                                    make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], k),
+                                                __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                const float2 up =
+                                    make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], k),
+                                                __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
+                            }
+                            const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
+                            const float2 c = make_float2(cand[(pl - N) % (N + 1)][2 * op],
+                                                         cand[(pl - N) % (N + 1)][2 * op + 1]);
+                            if constexpr (KAHAN) {
+                                kahan_add(zacc[op][q], w);
+                                kahan_add(nacc[op][q], __fmul2_rn(w, c));
+                            } else {
+                                zacc[op][q].s = __fadd2_rn(zacc[op][q].s, w);
+                                nacc[op][q].s = __ffma2_rn(w, c, nacc[op][q].s);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    const int x = X0 + lane - N;
+    if (lane >= N && lane < 32 - N && x < X) {
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) {
+            const int z = Z0 + q;
+            if (z >= Z) break;
+#pragma unroll
+            for (int r = 0; r < RY; ++r) {
+                const int y = Y0 + warp * RY + r;
+                if (y >= Y) break;
+                const size_t o = ((size_t)z * Y + y) * X + x;
+                const float2 zz = zacc[r / 2][q].s, nn = nacc[r / 2][q].s;
+                const float zs = (r & 1) ? zz.y : zz.x;
+                const float nm = (r & 1) ? nn.y : nn.x;
+                out[o] = nm / zs * inv_scale;
+                if (zsum) zsum[o] = zs;
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace gnlm

@@ -32,6 +32,14 @@ NLM_FLAG_PREPADDED = 0x2
 _lib = None
 
 
+class NLMVolume(ctypes.Structure):
+    """Mirror of struct nlm_volume in include/nlm.h."""
+    _fields_ = [("d_in", ctypes.c_void_p), ("in_dtype", ctypes.c_int), ("X", ctypes.c_int),
+                ("Y", ctypes.c_int), ("Z", ctypes.c_int), ("sr", ctypes.c_int),
+                ("pr", ctypes.c_int), ("h", ctypes.c_float), ("d_out", ctypes.c_void_p),
+                ("d_zsum", ctypes.c_void_p)]
+
+
 class NLMError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"nlm status {code}: {msg}")
@@ -66,6 +74,12 @@ def lib():
     L.nlm3d_adjoint_workspace_bytes.argtypes = [i, i, i, i, i]
     L.nlm3d_adjoint_workspace_bytes.restype = sz
     L.nlm3d_adjoint.argtypes = [vp, vp, vp, vp, i, i, i, i, i, f, vp, vp, vp, sz, vp]
+    L.nlm3d_batch_create.argtypes = [ctypes.POINTER(NLMVolume), i, u, ctypes.POINTER(vp)]
+    L.nlm3d_batch_run.argtypes = [vp, vp]
+    L.nlm3d_batch_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_float), vp]
+    L.nlm3d_batch_set_variant.argtypes = [vp, i]
+    L.nlm3d_batch_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(sz)]
+    L.nlm3d_batch_destroy.argtypes = [vp]
     L.nlm_variant_count.argtypes = [i, u]
     L.nlm_set_variant.argtypes = [i, i, i, u, i]
     L.nlm_get_variant.argtypes = [i, i, i, u]
@@ -191,6 +205,58 @@ def nlm3d_adjoint(x, out, zsum, gout, sr, pr, h, gin=None, hgrad=None, workspace
                               float(h), _ptr(gin), _ptr(hgrad), ws_ptr, ws_bytes,
                               _stream_ptr(stream)))
     return gin, hgrad
+
+
+class BatchPlan:
+    """A batched 3D plan over CUDA tensors (one persistent, graph-captured launch).
+
+    ``volumes`` is a list of (tensor [Z, Y, X], sr, pr, h); outputs are allocated here.
+    """
+
+    N_VARIANTS = 3
+
+    def __init__(self, volumes, with_zsum=False):
+        torch = _torch()
+        self.inputs = [v[0].contiguous() for v in volumes]
+        self.outputs = [torch.empty(t.shape, dtype=torch.float32, device=t.device)
+                        for t in self.inputs]
+        self.zsums = [torch.empty_like(o) for o in self.outputs] if with_zsum else None
+        arr = (NLMVolume * len(volumes))()
+        for k, ((t, sr, pr, h), x, o) in enumerate(zip(volumes, self.inputs, self.outputs)):
+            Z, Y, X = x.shape
+            arr[k] = NLMVolume(x.data_ptr(), _dtype_code(x), X, Y, Z, sr, pr, float(h),
+                               o.data_ptr(), self.zsums[k].data_ptr() if with_zsum else None)
+        self._arr = arr
+        self.handle = ctypes.c_void_p()
+        check(lib().nlm3d_batch_create(arr, len(volumes), 0, ctypes.byref(self.handle)))
+
+    def run(self, stream=None):
+        check(lib().nlm3d_batch_run(self.handle, _stream_ptr(stream)))
+        return self.outputs
+
+    def autotune(self, stream=None):
+        times = (ctypes.c_float * self.N_VARIANTS)()
+        best = check_nonneg(lib().nlm3d_batch_autotune(self.handle, times, _stream_ptr(stream)))
+        return best, list(times)
+
+    def set_variant(self, v):
+        check(lib().nlm3d_batch_set_variant(self.handle, int(v)))
+
+    def info(self):
+        n, v, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+        check(lib().nlm3d_batch_info(self.handle, ctypes.byref(n), ctypes.byref(v), ctypes.byref(b)))
+        return {"items": n.value, "variant": v.value, "device_bytes": b.value}
+
+    def close(self):
+        if self.handle:
+            lib().nlm3d_batch_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def variant_count(dims, fp16_storage=False):

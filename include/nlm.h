@@ -149,6 +149,41 @@ int nlm3d_adjoint(const float* d_in, const float* d_out, const float* d_zsum, co
                   int X, int Y, int Z, int sr, int pr, float h, float* d_gin, double* d_hgrad,
                   void* d_ws, size_t ws_bytes, nlm_stream_t stream);
 
+/* -------------------------------------------------------------- batched -- */
+
+/* One volume of a batch: device pointers owned by the caller, kept alive and
+ * unchanged in address for the life of the plan (their contents may change). */
+typedef struct nlm_volume {
+    const void* d_in;  /* X*Y*Z elements of in_dtype, unpadded */
+    int in_dtype;
+    int X, Y, Z;
+    int sr, pr;        /* batched form: pr = 1, sr in 1..5 */
+    float h;
+    float* d_out;      /* X*Y*Z floats */
+    float* d_zsum;     /* nullable */
+} nlm_volume;
+
+typedef struct nlm_batch_plan nlm_batch_plan;
+
+/*
+ * Many volumes of uneven sizes, each with its own h and search radius, denoised
+ * by one persistent kernel launch (no counterpart in the reference, whose sweeps
+ * rerun one compile-time configuration at a time, 3DNLM/run.sh:25-34).
+ * nlm3d_batch_create stages nothing yet; it allocates the plan's device memory
+ * (staged copies, descriptor tables, work list), builds the tile work list (most
+ * expensive first) and captures a CUDA graph [reset work counter -> stage all
+ * volumes -> persistent NLM kernel].  nlm3d_batch_run replays the graph on
+ * `stream` (asynchronous).  nlm3d_batch_autotune times each tile shape on the
+ * batch, keeps the fastest, and returns its index (times_ms: one entry per shape,
+ * nullable).  flags must be 0 (FP32).
+ */
+int nlm3d_batch_create(const nlm_volume* vols, int n, unsigned int flags, nlm_batch_plan** plan);
+int nlm3d_batch_run(nlm_batch_plan* plan, nlm_stream_t stream);
+int nlm3d_batch_autotune(nlm_batch_plan* plan, float* times_ms, nlm_stream_t stream);
+int nlm3d_batch_set_variant(nlm_batch_plan* plan, int variant);
+int nlm3d_batch_info(const nlm_batch_plan* plan, int* n_items, int* variant, size_t* device_bytes);
+int nlm3d_batch_destroy(nlm_batch_plan* plan);
+
 /* ------------------------------------------------------------ autotuner -- */
 
 /*
