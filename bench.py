@@ -164,6 +164,100 @@ def cpu_baseline(shape, budget_s=10.0):
                       f"(reflect borders at the slab ends), {dt:.1f} s"}
 
 
+def bench_batched(torch, gnlm, reps=3):
+    """64 uneven volumes (dims in {32..192}, sr 3 for half and 5 for the other
+    half, pr 1, h = sigma): one graph-captured persistent launch against 64
+    sequential single-volume launches on the same stream, both device-timed."""
+    from gnlm import phantom
+    specs = phantom.batch_specs()
+    vols = [(torch.from_numpy(v).cuda(), s["sr"], 1, s["h"])
+            for v, s in zip(phantom.batch_volumes(specs), specs)]
+    nvox = sum(t.numel() for t, *_ in vols)
+    plan = gnlm.BatchPlan(vols)
+    best, tune_ms = plan.autotune()
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return min(ms)
+
+    batch_ms = timed(plan.run)
+    outs = [torch.empty_like(t) for t, *_ in vols]
+
+    def sequential():
+        for (t, sr, pr, h), o in zip(vols, outs):
+            gnlm.nlm3d_forward(t, sr, pr, h, out=o)
+
+    seq_ms = timed(sequential)
+    same = max(float((a - b).abs().max()) for a, b in zip(plan.outputs, outs))
+    info = plan.info()
+    plan.close()
+    return {"volumes": len(vols), "voxels": nvox, "work_items": info["items"],
+            "value": round(nvox / (batch_ms * 1e-3) / 1e6, 2), "ms": round(batch_ms, 3),
+            "sequential_value": round(nvox / (seq_ms * 1e-3) / 1e6, 2),
+            "sequential_ms": round(seq_ms, 3), "speedup_vs_sequential": round(seq_ms / batch_ms, 3),
+            "variant": best, "autotune_ms": [round(t, 3) for t in tune_ms],
+            "max_abs_diff_vs_sequential": same}
+
+
+def bench_adjoint(torch, gnlm, steps=50):
+    """128^3 (ellipsoids, sigma 0.05, sr 3, pr 1): forward + adjoint per step, used
+    to fit h by gradient descent on the MSE to the clean phantom."""
+    from gnlm import phantom
+    noisy, clean = phantom.ellipsoid_phantom((128, 128, 128), n_ellipsoids=16, sigma=0.05, seed=4)
+    x, c = torch.from_numpy(noisy).cuda(), torch.from_numpy(clean).cuda()
+    n = x.numel()
+    ws = torch.empty(gnlm.lib().nlm3d_adjoint_workspace_bytes(128, 128, 128, SR, PR),
+                     dtype=torch.uint8, device="cuda")
+    out, zs, gin = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    hg = torch.zeros(1, dtype=torch.float64, device="cuda")
+    g = torch.randn(x.shape, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+    stream = torch.cuda.current_stream()
+    for _ in range(2):  # warm-up
+        gnlm.nlm3d_forward(x, SR, PR, 0.05, out=out, zsum=zs, return_zsum=True)
+        gnlm.nlm3d_adjoint(x, out, zs, g, SR, PR, 0.05, gin=gin, hgrad=hg, workspace=ws)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
+    gnlm.nlm3d_forward(x, SR, PR, 0.05, out=out, zsum=zs, return_zsum=True)
+    ev[1].record(stream)
+    gnlm.nlm3d_adjoint(x, out, zs, g, SR, PR, 0.05, gin=gin, hgrad=hg, workspace=ws)
+    ev[2].record(stream)
+    ev[2].synchronize()
+    fwd_ms, adj_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    # h fit: 50 steps of normalised gradient descent on MSE(out(h), clean)
+    h = 0.02
+    mse0 = None
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        gnlm.nlm3d_forward(x, SR, PR, h, out=out, zsum=zs, return_zsum=True)
+        diff = out - c
+        gout = diff * (2.0 / n)
+        gnlm.nlm3d_adjoint(x, out, zs, gout, SR, PR, h, gin=gin, hgrad=hg, workspace=ws)
+        mse = float((diff * diff).mean())  # host read of the step's loss
+        mse0 = mse if mse0 is None else mse0
+        grad = float(hg.item())
+        h = max(1e-3, h - 0.002 * (1.0 if grad > 0 else -1.0))
+    t1.record(stream)
+    t1.synchronize()
+    return {"shape": [128, 128, 128], "search_radius": SR, "patch_radius": PR,
+            "fwd_ms": round(fwd_ms, 3), "adjoint_ms": round(adj_ms, 3),
+            "fwd_adjoint_ms_per_step": round(fwd_ms + adj_ms, 3),
+            "h_fit": {"steps": steps, "h0": 0.02, "h": round(h, 4), "mse0": mse0, "mse": mse,
+                      "ms_per_step_with_loss_readback": round(t0.elapsed_time(t1) / steps, 3)}}
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -174,7 +268,9 @@ def run_reference(args):
     O.set_threads(threads)
     vol, _ = phantom.ellipsoid_phantom(SHAPE, n_ellipsoids=N_ELLIPSOIDS, sigma=SIGMA, seed=SEED)
     Z, Y, X = SHAPE
-    nz = 8
+    # 64 planes: the oracle parallelises over 4-plane z chunks, so this keeps every
+    # host thread busy (16 chunks) while one step stays well under a second
+    nz = 64
     slab = np.ascontiguousarray(vol[Z // 2 - nz // 2:Z // 2 + nz // 2])
     for _ in range(args.warmup):
         O.nlm3d(slab, SR, PR, H)
@@ -306,6 +402,8 @@ def run_gnlm(args):
 
     peak = fp32_peak_tflops(torch)
     peak_x2 = fp32_peak_tflops(torch, packed=True)
+    batched = bench_batched(torch, gnlm) if not args.skip_extra else None
+    adjoint = bench_adjoint(torch, gnlm) if not args.skip_extra else None
     fused_mean = statistics.mean(fused_ms)
     achieved = FLOPS_PER_PAIR * OFFSETS * nvox / (fused_mean * 1e-3) / 1e12
     traffic = read_profile_traffic("nlm3d_fwd_kernel")
@@ -335,7 +433,9 @@ def run_gnlm(args):
                        "fused_fp32": round(fused_mean, 4),
                        "fused_fp16": round(statistics.mean(f16), 4)},
         "forms": {"fp32": {"value": round(value, 2), "max_abs_err_vs_fp64": err32},
-                  "fp16_storage": {"value": round(fp16_value, 2), "max_abs_err_vs_fp64": err16}},
+                  "fp16_storage": {"value": round(fp16_value, 2), "max_abs_err_vs_fp64": err16},
+                  "batched": batched},
+        "adjoint": adjoint,
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:
@@ -353,6 +453,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gnlm", "reference"], default="gnlm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-extra", action="store_true",
+                    help="skip the batched and adjoint workloads (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
