@@ -26,6 +26,49 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                                                   errword);
 }
 
+// FP16-storage single-volume kernel (row-pair layout, two tensor maps).
+template <int M, int N, int RY, int RZ, int NW, int MINB, bool KAHAN>
+__global__ void __launch_bounds__(32 * NW, MINB)
+    nlm3d_fwd_h2_kernel(const __grid_constant__ CUtensorMap mapE,
+                        const __grid_constant__ CUtensorMap mapO, int X, int Y, int Z,
+                        float inv_scale, float* __restrict__ out, float* __restrict__ zsum,
+                        unsigned int* errword) {
+    using C = Fwd3dH2<M, N, RY, RZ, NW>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    fwd3d_tile_h2<M, N, RY, RZ, NW, KAHAN>(&mapE, &mapO, smem_raw, bar, 0, blockIdx.x,
+                                           blockIdx.y, blockIdx.z, X, Y, Z, inv_scale, out, zsum,
+                                           errword);
+}
+
+template <int M, int N, int RY, int RZ, int NW, int MINB, bool KAHAN>
+static cudaError_t run_fwd3d_h2(const Staging& st, const void* staged, float inv_scale,
+                                float* out, float* zsum, unsigned int* errword,
+                                cudaStream_t stream) {
+    using C = Fwd3dH2<M, N, RY, RZ, NW>;
+    CUtensorMap mapE, mapO;
+    const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yq, (uint64_t)st.Zp};
+    const uint64_t strides[2] = {(uint64_t)st.Xs * 4, (uint64_t)st.Xs * st.Yq * 4};
+    const uint32_t box[3] = {(uint32_t)C::BX, (uint32_t)C::BYQ, (uint32_t)C::BZ};
+    char* base = static_cast<char*>(const_cast<void*>(staged));
+    cudaError_t e = encode_tensor_map(&mapE, false, 3, dims, strides, box, base);
+    if (e == cudaSuccess)
+        e = encode_tensor_map(&mapO, false, 3, dims, strides, box, base + st.copy_bytes());
+    if (e != cudaSuccess) return e;
+    auto kern = nlm3d_fwd_h2_kernel<M, N, RY, RZ, NW, MINB, KAHAN>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY, (st.Z + RZ - 1) / RZ);
+    kern<<<grid, 32 * NW, C::SMEM_BYTES, stream>>>(mapE, mapO, st.X, st.Y, st.Z, inv_scale, out,
+                                                   zsum, errword);
+    return cudaGetLastError();
+}
+
 template <int M, int N, typename T, int RY, int RZ, int NW, int MINB, bool AREG, bool KAHAN>
 static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_scale, float* out,
                              float* zsum, unsigned int* errword, cudaStream_t stream) {
@@ -55,8 +98,8 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
 //   1: 4 x 8, reference values re-read from shared memory, 3 CTAs/SM
 //   2: 4 x 4, registers, 3 CTAs/SM
 //   3: 2 x 8, registers, 3 CTAs/SM
-// FP16-storage form (Kahan-compensated sums):
-//   0: 4 x 4, registers, 3 CTAs/SM;  1: 4 x 8, shared memory, 2 CTAs/SM;  2: 2 x 8, registers
+// FP16-storage form (row-pair layout, Kahan-compensated weight sum):
+//   0: 4 x 8, 2 CTAs/SM;  1: 4 x 4, 3 CTAs/SM;  2: 2 x 8, 3 CTAs/SM
 template <int m, int n>
 static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16, int v,
                                float inv_scale, float* out, float* zsum, unsigned int* ew,
@@ -70,9 +113,9 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
         }
     } else {
         switch (v) {
-            case 0: return run_fwd3d<m, n, __half, 4, 4, 4, 3, true, true>(st, staged, inv_scale, out, zsum, ew, s);
-            case 1: return run_fwd3d<m, n, __half, 4, 8, 4, 2, false, true>(st, staged, inv_scale, out, zsum, ew, s);
-            case 2: return run_fwd3d<m, n, __half, 2, 8, 4, 3, true, true>(st, staged, inv_scale, out, zsum, ew, s);
+            case 0: return run_fwd3d_h2<m, n, 4, 8, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s);
+            case 1: return run_fwd3d_h2<m, n, 4, 4, 4, 3, true>(st, staged, inv_scale, out, zsum, ew, s);
+            case 2: return run_fwd3d_h2<m, n, 2, 8, 4, 3, true>(st, staged, inv_scale, out, zsum, ew, s);
         }
     }
     return cudaErrorInvalidValue;

@@ -245,4 +245,194 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// FP16-storage form (precision form).  The staged volume is the row-pair layout
+// (two copies of half2 pairs, see Staging::pairs), so one 32-bit shared load gives
+// a candidate voxel of two adjacent rows: half the shared-memory traffic of FP32.
+// Differences are formed in FP16 (one HSUB2 per row pair), converted, and every
+// square and sum after that is FP32.  The weight sum Z is Kahan-compensated; the
+// weighted sum is kept as T = sum w t_c with t_c = v_p - v_{p+o}, so that
+// out = v_p - T / Z needs no conversion of candidate values.
+template <int M, int N, int RY, int RZ, int NW>
+struct Fwd3dH2 {
+    static constexpr int H = M + N;
+    static constexpr int XO = 32 - 2 * N;
+    static constexpr int RMAX = 4 - cgcd(XO, 4);
+    static constexpr int BX = cround(32 + 2 * M + RMAX, 4);  // half2 columns
+    static constexpr int TY = NW * RY;
+    static constexpr int BYQ = TY / 2 + H;                    // row pairs per copy
+    static constexpr int BZ = RZ + 2 * H;
+    static constexpr int PLANEQ = BX * BYQ;
+    static constexpr int COPY_BYTES = BX * BYQ * BZ * 4;
+    static constexpr int COPY_STRIDE = cround(COPY_BYTES, 128);  // TMA destination alignment
+    static constexpr int BAR_OFF = 2 * COPY_STRIDE;
+    static constexpr int SMEM_BYTES = BAR_OFF + 128;
+    static constexpr int K = 2 * N + 1;
+    static constexpr int ROWS = RY + 2 * N;
+    static constexpr int PLANES = RZ + 2 * N;
+    static_assert(BX <= 256 && BYQ <= 256 && BZ <= 256, "TMA box dimension > 256");
+    static_assert(COPY_STRIDE % 128 == 0, "TMA destination alignment");
+    static_assert(SMEM_BYTES <= 227 * 1024, "tile exceeds shared memory");
+    static_assert(RY % 2 == 0 && (NW * RY) % 2 == 0, "row pairs");
+};
+
+template <int M, int N, int RY, int RZ, int NW, bool KAHAN>
+__device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUtensorMap* mapO,
+                                              unsigned char* smem, uint64_t* bar, uint32_t parity,
+                                              int bx, int by, int bz, int X, int Y, int Z,
+                                              float inv_scale, float* __restrict__ out,
+                                              float* __restrict__ zsum, unsigned int* errword) {
+    using C = Fwd3dH2<M, N, RY, RZ, NW>;
+    constexpr int RP = C::ROWS / 2;
+    constexpr int OP = RY / 2;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int X0 = bx * C::XO, Y0 = by * C::TY, Z0 = bz * RZ;
+    const int xs = X0 & ~3;
+    const int ral = X0 - xs;
+    const __half2* E = reinterpret_cast<const __half2*>(smem);
+    const __half2* O = reinterpret_cast<const __half2*>(smem + C::COPY_STRIDE);
+
+    if (threadIdx.x == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, 2 * C::COPY_BYTES);
+        // E pair k = rows (2k, 2k+1) from pair Y0/2; O pair k = rows (2k+1, 2k+2) from Y0/2 - 1
+        tma_load_3d(smem, mapE, xs, Y0 / 2, Z0, bar);
+        tma_load_3d(smem + C::COPY_STRIDE, mapO, xs, Y0 / 2 - 1, Z0, bar);
+    }
+    if (!mbar_wait_bounded(bar, parity)) {
+        if (threadIdx.x == 0) {
+            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
+            mbar_wait_bounded(bar, parity);
+        }
+        return false;
+    }
+
+    // Row pair (r, r+1) of the tile, r = Y0 + j: in E at index j/2 if r is even, in O at
+    // (j+1)/2 if odd.  The thread's rows start at j = warp*RY + M (+ oy for candidates).
+    const int col = lane + M + ral;
+    const int j0 = warp * RY + M;
+    const __half2* abase = (M & 1) ? O + ((j0 + 1) >> 1) * C::BX : E + (j0 >> 1) * C::BX;
+    abase += (C::H - N) * C::PLANEQ + col;
+    __half2 areg[C::PLANES][RP];
+#pragma unroll
+    for (int pl = 0; pl < C::PLANES; ++pl)
+#pragma unroll
+        for (int rp = 0; rp < RP; ++rp) areg[pl][rp] = abase[pl * C::PLANEQ + rp * C::BX];
+
+    Kahan2 zacc[OP][RZ];
+    float tacc[RY][RZ];
+#pragma unroll
+    for (int r = 0; r < OP; ++r)
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) zacc[r][q].s = zacc[r][q].c = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < RY; ++r)
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) tacc[r][q] = 0.f;
+
+    for (int oy = -M; oy <= M; ++oy) {
+        const int jb = j0 + oy;  // >= 0
+        const __half2* brow = ((M + oy) & 1) ? O + ((jb + 1) >> 1) * C::BX : E + (jb >> 1) * C::BX;
+        for (int oz = -M; oz <= M; ++oz) {
+            for (int ox = -M; ox <= M; ++ox) {
+                const __half2* bptr = brow + (C::H - N + oz) * C::PLANEQ + col + ox;
+                float2 S[RP];
+                float2 tr[C::K][RP];
+#pragma unroll
+                for (int pl = 0; pl < C::PLANES; ++pl) {
+#pragma unroll
+                    for (int rp = 0; rp < RP; ++rp) {
+                        const __half2 b2 = bptr[pl * C::PLANEQ + rp * C::BX];
+                        const float2 t = __half22float2(__hsub2(areg[pl][rp], b2));
+                        if (pl == 0)
+                            S[rp] = __fmul2_rn(t, t);
+                        else
+                            S[rp] = __ffma2_rn(t, t, S[rp]);
+                        if (pl >= C::K) {
+                            const float2 to = tr[(pl - C::K) % C::K][rp];
+                            S[rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S[rp]);
+                        }
+                        tr[pl % C::K][rp] = t;
+                    }
+                    if (pl >= 2 * N) {
+                        const int q = pl - 2 * N;
+                        float Srow[C::ROWS], tc[C::ROWS];
+#pragma unroll
+                        for (int rp = 0; rp < RP; ++rp) {
+                            Srow[2 * rp] = S[rp].x;
+                            Srow[2 * rp + 1] = S[rp].y;
+                            const float2 c2 = tr[(pl - N) % C::K][rp];  // centre plane q + N
+                            tc[2 * rp] = c2.x;
+                            tc[2 * rp + 1] = c2.y;
+                        }
+                        float Yv[RY];
+                        if constexpr (N == 1) {
+#pragma unroll
+                            for (int r = 0; r < RY; r += 2) {
+                                const float u = Srow[r + 1] + Srow[r + 2];
+                                Yv[r] = Srow[r] + u;
+                                Yv[r + 1] = u + Srow[r + 3];
+                            }
+                        } else {
+                            float acc = 0.f;
+#pragma unroll
+                            for (int k = 0; k < C::K; ++k) acc += Srow[k];
+                            Yv[0] = acc;
+#pragma unroll
+                            for (int r = 1; r < RY; ++r) {
+                                acc = acc + Srow[r + C::K - 1] - Srow[r - 1];
+                                Yv[r] = acc;
+                            }
+                        }
+#pragma unroll
+                        for (int op = 0; op < OP; ++op) {
+                            float2 xv = make_float2(Yv[2 * op], Yv[2 * op + 1]);
+#pragma unroll
+                            for (int k = 1; k <= N; ++k) {
+                                const float2 dn =
+                                    make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], k),
+                                                __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                const float2 up =
+                                    make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], k),
+                                                __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
+                            }
+                            const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
+                            if constexpr (KAHAN)
+                                kahan_add(zacc[op][q], w);
+                            else
+                                zacc[op][q].s = __fadd2_rn(zacc[op][q].s, w);
+                            tacc[2 * op][q] = fmaf(w.x, tc[2 * op + N], tacc[2 * op][q]);
+                            tacc[2 * op + 1][q] = fmaf(w.y, tc[2 * op + 1 + N], tacc[2 * op + 1][q]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    const int x = X0 + lane - N;
+    if (lane >= N && lane < 32 - N && x < X) {
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) {
+            const int z = Z0 + q;
+            if (z >= Z) break;
+#pragma unroll
+            for (int r = 0; r < RY; ++r) {
+                const int y = Y0 + warp * RY + r;
+                if (y >= Y) break;
+                const size_t o = ((size_t)z * Y + y) * X + x;
+                const float2 zz = zacc[r / 2][q].s;
+                const float zs = (r & 1) ? zz.y : zz.x;
+                const __half2 a2 = areg[q + N][(r + N) / 2];  // reference value v_p
+                const float vp = ((r + N) & 1) ? __high2float(a2) : __low2float(a2);
+                out[o] = (vp - tacc[r][q] / zs) * inv_scale;
+                if (zsum) zsum[o] = zs;
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace gnlm

@@ -113,6 +113,11 @@ int resolve_ws(void** d_ws, size_t* ws_bytes, size_t need, cudaStream_t stream) 
     return NLM_OK;
 }
 
+// 3D staging: FP32 layout, or the row-pair layout for FP16 storage.
+Staging staging3d(int X, int Y, int Z, int H, bool fp16) {
+    return fp16 ? make_staging_pairs(X, Y, Z, H) : make_staging(X, Y, Z, H, H, false);
+}
+
 float weight_scale(int pr, int dims, float h) {
     const double k = 2.0 * pr + 1.0;
     const double P = dims == 3 ? k * k * k : k * k;
@@ -249,7 +254,7 @@ int nlm_release_cached(void) {
 size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags) {
     if (X < 1 || Y < 1 || Z < 1 || sr < 0 || pr < 0) return 0;
     const int H = sr + pr;
-    return make_staging(X, Y, Z, H, H, (flags & NLM_FLAG_FP16_STORAGE) != 0).bytes();
+    return staging3d(X, Y, Z, H, (flags & NLM_FLAG_FP16_STORAGE) != 0).bytes();
 }
 
 static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
@@ -259,7 +264,7 @@ static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
     if (!nlm3d_fwd_supported(sr, pr, fp16))
         return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
-    Staging st = make_staging(X, Y, Z, H, H, fp16);
+    Staging st = staging3d(X, Y, Z, H, fp16);
     int rc = resolve_ws(d_ws, ws_bytes, st.bytes(), stream);
     if (rc) return rc;
     cudaError_t e = launch_stage(d_in, in_dtype, (flags & NLM_FLAG_PREPADDED) != 0,
@@ -273,7 +278,7 @@ static int fwd3d_staged_impl(const void* d_ws, int X, int Y, int Z, int sr, int 
                              cudaStream_t stream) {
     const int H = sr + pr;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
-    Staging st = make_staging(X, Y, Z, H, H, fp16);
+    Staging st = staging3d(X, Y, Z, H, fp16);
     cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, tuned_variant(3, sr, pr, fp16),
                                      1.0f / weight_scale(pr, 3, h), d_out, d_zsum,
                                      device_error_word(), stream);
@@ -418,7 +423,7 @@ int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int fla
     if (rc) return rc;
     if (!nlm3d_fwd_supported(sr, pr, fp16))
         return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
-    const Staging st = make_staging(X, Y, Z, sr + pr, sr + pr, fp16);
+    const Staging st = staging3d(X, Y, Z, sr + pr, fp16);
     const size_t nvox = (size_t)X * Y * Z;
     void *d_in = nullptr, *d_ws = nullptr;
     float* d_out = nullptr;

@@ -17,16 +17,29 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // get the base-2 exponent of the weight directly as a sum of squared
 // differences.  Layout [Zp][Yp][Xs], x stride Xs a multiple of 16 bytes (the
 // TMA global-stride rule).
+//
+// 3D FP16 storage uses the row-pair layout instead (pairs = true): two copies,
+// E and O, each [Zp][Yq][Xs] of half2, where E pair k holds padded rows (2k, 2k+1)
+// and O pair k holds rows (2k+1, 2k+2) (zero past the last row).  One 32-bit
+// load then yields one voxel of two adjacent rows, whichever row a search offset
+// starts on.
 struct Staging {
     int X = 0, Y = 0, Z = 0;  // unpadded extents
     int H = 0, Hz = 0;        // halo in x/y and in z
     int Xp = 0, Yp = 0, Zp = 0;
     int Xs = 0;               // x stride in elements
-    int elem = 4;             // 4 (FP32) or 2 (FP16)
-    size_t bytes() const { return align_up((size_t)Xs * Yp * Zp * elem, kAlign); }
+    int elem = 4;             // 4 (FP32, or a half2 pair), 2 (FP16)
+    bool pairs = false;       // row-pair FP16 layout (two copies)
+    int Yq = 0;               // row pairs per copy
+    size_t copy_bytes() const { return align_up((size_t)Xs * Yq * Zp * 4, kAlign); }
+    size_t bytes() const {
+        return pairs ? 2 * copy_bytes() : align_up((size_t)Xs * Yp * Zp * elem, kAlign);
+    }
 };
 
 Staging make_staging(int X, int Y, int Z, int H, int Hz, bool fp16);
+// 3D FP16-storage staging (row-pair layout).
+Staging make_staging_pairs(int X, int Y, int Z, int H);
 
 // Pads, converts and scales `in` into `dst` (layout of `st`).  in_dtype is an
 // nlm_dtype; with `prepadded` the input already has the halo (layout

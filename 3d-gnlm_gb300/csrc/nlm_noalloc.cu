@@ -13,9 +13,9 @@
 // The array is kNoAllocScratchBytes (16 MiB) of device memory.  Every GPU that loads
 // the library holds it until the process exits, whether or not this entry point is
 // ever called.  A call whose staged volume needs more (padded (X+2H)(Y+2H)(Z+2H)
-// voxels, H = sr + pr, 4 bytes each in FP32 or 2 in FP16 storage, x rows rounded up to
-// 16 bytes) is rejected with NLM_ERR_WORKSPACE: for sr 3, pr 1 that is up to 152^3 in
-// FP32 (about 160^3 padded) or 192^3 in FP16 storage.
+// voxels, H = sr + pr, 4 bytes each in FP32; FP16 storage keeps two row-paired copies
+// of 2 bytes per voxel, so about the same; x rows rounded up to 16 bytes) is rejected
+// with NLM_ERR_WORKSPACE: for sr 3, pr 1 that is up to 152^3 (about 160^3 padded).
 //
 // Every call on a device shares the one array, so calls whose GPU work overlaps (on two
 // streams, or from two threads) race on it: serialise them, for example on one stream.

@@ -29,6 +29,60 @@ Staging make_staging(int X, int Y, int Z, int H, int Hz, bool fp16) {
     return s;
 }
 
+Staging make_staging_pairs(int X, int Y, int Z, int H) {
+    Staging s = make_staging(X, Y, Z, H, H, false);
+    s.pairs = true;
+    s.elem = 4;
+    s.Xs = (s.Xp + 3) / 4 * 4;  // half2 elements, 16-byte rows
+    s.Yq = (s.Yp + 2) / 2;
+    return s;
+}
+
+// Row-pair layout: block = (pair k, plane, copy c); rows 2k+c and 2k+c+1.
+template <typename Tin, bool PREPADDED>
+__global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict__ in, int X, int Y,
+                                                          int Z, int H, int Xp, int Yp, int Xs,
+                                                          int Yq, size_t copy_elems, float scale,
+                                                          __half2* __restrict__ dst) {
+    const int k = blockIdx.x, pz = blockIdx.y, c = blockIdx.z;
+    const int r0 = 2 * k + c, r1 = r0 + 1;
+    __half2* drow = dst + c * copy_elems + ((size_t)pz * Yq + k) * Xs;
+    const Tin *s0 = nullptr, *s1 = nullptr;
+    if (PREPADDED) {
+        if (r0 < Yp) s0 = in + ((size_t)pz * Yp + r0) * Xp;
+        if (r1 < Yp) s1 = in + ((size_t)pz * Yp + r1) * Xp;
+    } else {
+        const int sz = reflect101(pz - H, Z);
+        if (r0 < Yp) s0 = in + ((size_t)sz * Y + reflect101(r0 - H, Y)) * X;
+        if (r1 < Yp) s1 = in + ((size_t)sz * Y + reflect101(r1 - H, Y)) * X;
+    }
+    for (int px = threadIdx.x; px < Xs; px += blockDim.x) {
+        float v0 = 0.f, v1 = 0.f;
+        if (px < Xp) {
+            const int sx = PREPADDED ? px : reflect101(px - H, X);
+            if (s0) v0 = to_f32(s0[sx]) * scale;
+            if (s1) v1 = to_f32(s1[sx]) * scale;
+        }
+        drow[px] = __floats2half2_rn(v0, v1);
+    }
+}
+
+template <typename Tin>
+static cudaError_t stage_pairs_typed(const void* in, bool prepadded, float scale, const Staging& st,
+                                     void* dst, cudaStream_t stream) {
+    dim3 grid(st.Yq, st.Zp, 2);
+    const size_t copy_elems = st.copy_bytes() / 4;
+    if (prepadded)
+        stage_pairs_kernel<Tin, true><<<grid, 256, 0, stream>>>(
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp, st.Yp, st.Xs, st.Yq, copy_elems, scale,
+            (__half2*)dst);
+    else
+        stage_pairs_kernel<Tin, false><<<grid, 256, 0, stream>>>(
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp, st.Yp, st.Xs, st.Yq, copy_elems, scale,
+            (__half2*)dst);
+    return cudaGetLastError();
+}
+
 // One block per padded row (blockIdx.x = row in [0, Yp), blockIdx.y = plane).
 template <typename Tin, typename Tout, bool PREPADDED>
 __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
@@ -71,6 +125,14 @@ static cudaError_t stage_typed(const void* in, bool prepadded, float scale, cons
 
 cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float scale,
                          const Staging& st, void* dst, cudaStream_t stream) {
+    if (st.pairs) {
+        switch (in_dtype) {
+            case NLM_U8: return stage_pairs_typed<unsigned char>(in, prepadded, scale, st, dst, stream);
+            case NLM_F16: return stage_pairs_typed<__half>(in, prepadded, scale, st, dst, stream);
+            case NLM_F32: return stage_pairs_typed<float>(in, prepadded, scale, st, dst, stream);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     const bool fp16 = st.elem == 2;
     switch (in_dtype) {
         case NLM_U8:

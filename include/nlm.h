@@ -114,8 +114,8 @@ int nlm3d_forward_staged(const void* d_ws, size_t ws_bytes, int X, int Y, int Z,
  * pipelines that reserve everything at start-up, where a cudaMalloc can fail
  * mid-run and a cudaFree stalls the whole device.  The staging scratch is a 16 MiB
  * array compiled into libgnlm.so, held on every GPU that loads the library until
- * the process exits.  Volumes whose staged copy needs more (sr 3, pr 1: beyond 152^3
- * in FP32, 192^3 with NLM_FLAG_FP16_STORAGE) return NLM_ERR_WORKSPACE.  The first
+ * the process exits.  Volumes whose staged copy needs more (sr 3, pr 1: beyond 152^3,
+ * FP32 or FP16 storage) return NLM_ERR_WORKSPACE.  The first
  * call on each device looks up the array's device address (make that first call
  * before any stream capture).  All calls on a device share the array: calls whose
  * GPU work overlaps race, so serialise them (e.g. on one stream).  The array keeps

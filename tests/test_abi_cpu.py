@@ -53,7 +53,8 @@ def test_workspace_query_is_pure_host(L):
     b16 = L.nlm3d_workspace_bytes(64, 64, 64, 3, 1, gnlm.NLM_FLAG_FP16_STORAGE)
     # padded 72^3, x stride rounded to 16 bytes, 256-byte aligned
     assert b32 == ((72 * 72 * 72 * 4 + 255) // 256) * 256
-    assert b16 == ((72 * 72 * 72 * 2 + 255) // 256) * 256
+    # FP16 storage: two row-pair copies (37 pairs of 72 padded rows) of half2
+    assert b16 == 2 * (((72 * 37 * 72 * 4) + 255) // 256) * 256
     assert L.nlm3d_workspace_bytes(0, 64, 64, 3, 1, 0) == 0
     assert L.nlm2d_workspace_bytes(2048, 2048, 5, 2, 0) == ((2064 * 2062 * 4 + 255) // 256) * 256
 
