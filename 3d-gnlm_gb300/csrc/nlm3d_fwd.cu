@@ -99,7 +99,7 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
 //   2: 4 x 4, registers, 3 CTAs/SM
 //   3: 2 x 8, registers, 3 CTAs/SM
 // FP16-storage form (row-pair layout, Kahan-compensated weight sum):
-//   0: 4 x 8, 2 CTAs/SM;  1: 4 x 4, 3 CTAs/SM;  2: 2 x 8, 3 CTAs/SM
+//   0: 4 x 6, 2 CTAs/SM;  1: 4 x 8, 2 CTAs/SM;  2: 2 x 8, 3 CTAs/SM
 template <int m, int n>
 static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16, int v,
                                float inv_scale, float* out, float* zsum, unsigned int* ew,
@@ -113,8 +113,8 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
         }
     } else {
         switch (v) {
-            case 0: return run_fwd3d_h2<m, n, 4, 8, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s);
-            case 1: return run_fwd3d_h2<m, n, 4, 4, 4, 3, true>(st, staged, inv_scale, out, zsum, ew, s);
+            case 0: return run_fwd3d_h2<m, n, 4, 6, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s);
+            case 1: return run_fwd3d_h2<m, n, 4, 8, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s);
             case 2: return run_fwd3d_h2<m, n, 2, 8, 4, 3, true>(st, staged, inv_scale, out, zsum, ew, s);
         }
     }

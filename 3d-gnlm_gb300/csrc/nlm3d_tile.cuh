@@ -249,10 +249,13 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
 // FP16-storage form (precision form).  The staged volume is the row-pair layout
 // (two copies of half2 pairs, see Staging::pairs), so one 32-bit shared load gives
 // a candidate voxel of two adjacent rows: half the shared-memory traffic of FP32.
-// Differences are formed in FP16 (one HSUB2 per row pair), converted, and every
-// square and sum after that is FP32.  The weight sum Z is Kahan-compensated; the
-// weighted sum is kept as T = sum w t_c with t_c = v_p - v_{p+o}, so that
-// out = v_p - T / Z needs no conversion of candidate values.
+// Reference values are held as FP32 in registers; each difference is one
+// mixed-precision subtraction (FP16 candidate, FP32 reference, FP32 result), so
+// no conversion instructions are needed and every square and sum is FP32.  The
+// weight sum Z is Kahan-compensated; the weighted sum is kept as
+// T = sum w (v_{p+o} - v_p), so that out = v_p + T / Z.  The weights of each
+// run of 2M+1 offsets (the innermost x loop) are summed plainly and the run sums
+// are added with Kahan compensation.
 template <int M, int N, int RY, int RZ, int NW>
 struct Fwd3dH2 {
     static constexpr int H = M + N;
@@ -275,6 +278,17 @@ struct Fwd3dH2 {
     static_assert(SMEM_BYTES <= 227 * 1024, "tile exceeds shared memory");
     static_assert(RY % 2 == 0 && (NW * RY) % 2 == 0, "row pairs");
 };
+
+// (b_lo - a0, b_hi - a1) in FP32 from a half2 of candidates and FP32 references:
+// PTX sub.rn.f32.f16 converts the f16 operand and subtracts in FP32 (one op each).
+__device__ __forceinline__ float2 sub_f32_f16x2(__half2 b2, float a0, float a1) {
+    float2 r;
+    asm("{\n\t.reg .f16 lo, hi;\n\tmov.b32 {lo, hi}, %2;\n\t"
+        "sub.rn.f32.f16 %0, lo, %3;\n\tsub.rn.f32.f16 %1, hi, %4;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "r"(*reinterpret_cast<const unsigned int*>(&b2)), "f"(a0), "f"(a1));
+    return r;
+}
 
 template <int M, int N, int RY, int RZ, int NW, bool KAHAN>
 __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUtensorMap* mapO,
@@ -314,11 +328,11 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
     const int j0 = warp * RY + M;
     const __half2* abase = (M & 1) ? O + ((j0 + 1) >> 1) * C::BX : E + (j0 >> 1) * C::BX;
     abase += (C::H - N) * C::PLANEQ + col;
-    __half2 areg[C::PLANES][RP];
+    float2 areg[C::PLANES][RP];
 #pragma unroll
     for (int pl = 0; pl < C::PLANES; ++pl)
 #pragma unroll
-        for (int rp = 0; rp < RP; ++rp) areg[pl][rp] = abase[pl * C::PLANEQ + rp * C::BX];
+        for (int rp = 0; rp < RP; ++rp) areg[pl][rp] = __half22float2(abase[pl * C::PLANEQ + rp * C::BX]);
 
     Kahan2 zacc[OP][RZ];
     float tacc[RY][RZ];
@@ -335,6 +349,13 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
         const int jb = j0 + oy;  // >= 0
         const __half2* brow = ((M + oy) & 1) ? O + ((jb + 1) >> 1) * C::BX : E + (jb >> 1) * C::BX;
         for (int oz = -M; oz <= M; ++oz) {
+            // plain packed sums of the weights over this run of 2M+1 offsets, folded into
+            // the Kahan-compensated total once per run
+            float2 zrun[OP][RZ];
+#pragma unroll
+            for (int r = 0; r < OP; ++r)
+#pragma unroll
+                for (int q = 0; q < RZ; ++q) zrun[r][q] = make_float2(0.f, 0.f);
             for (int ox = -M; ox <= M; ++ox) {
                 const __half2* bptr = brow + (C::H - N + oz) * C::PLANEQ + col + ox;
                 float2 S[RP];
@@ -344,7 +365,8 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
 #pragma unroll
                     for (int rp = 0; rp < RP; ++rp) {
                         const __half2 b2 = bptr[pl * C::PLANEQ + rp * C::BX];
-                        const float2 t = __half22float2(__hsub2(areg[pl][rp], b2));
+                        // t = v_{p+o} - v_p (sign is irrelevant to the squares)
+                        const float2 t = sub_f32_f16x2(b2, areg[pl][rp].x, areg[pl][rp].y);
                         if (pl == 0)
                             S[rp] = __fmul2_rn(t, t);
                         else
@@ -399,16 +421,22 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
                                 xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
                             }
                             const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
-                            if constexpr (KAHAN)
-                                kahan_add(zacc[op][q], w);
-                            else
-                                zacc[op][q].s = __fadd2_rn(zacc[op][q].s, w);
+                            zrun[op][q] = __fadd2_rn(zrun[op][q], w);
                             tacc[2 * op][q] = fmaf(w.x, tc[2 * op + N], tacc[2 * op][q]);
                             tacc[2 * op + 1][q] = fmaf(w.y, tc[2 * op + 1 + N], tacc[2 * op + 1][q]);
                         }
                     }
                 }
             }
+#pragma unroll
+            for (int r = 0; r < OP; ++r)
+#pragma unroll
+                for (int q = 0; q < RZ; ++q) {
+                    if constexpr (KAHAN)
+                        kahan_add(zacc[r][q], zrun[r][q]);
+                    else
+                        zacc[r][q].s = __fadd2_rn(zacc[r][q].s, zrun[r][q]);
+                }
         }
     }
 
@@ -425,9 +453,9 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
                 const size_t o = ((size_t)z * Y + y) * X + x;
                 const float2 zz = zacc[r / 2][q].s;
                 const float zs = (r & 1) ? zz.y : zz.x;
-                const __half2 a2 = areg[q + N][(r + N) / 2];  // reference value v_p
-                const float vp = ((r + N) & 1) ? __high2float(a2) : __low2float(a2);
-                out[o] = (vp - tacc[r][q] / zs) * inv_scale;
+                const float2 a2 = areg[q + N][(r + N) / 2];  // reference value v_p
+                const float vp = ((r + N) & 1) ? a2.y : a2.x;
+                out[o] = (vp + tacc[r][q] / zs) * inv_scale;
                 if (zsum) zsum[o] = zs;
             }
         }
