@@ -41,11 +41,49 @@ struct Fwd2d {
     static_assert(BAR_OFF % 128 == 0, "the tile (at offset 0) and barrier stay 128-byte aligned");
 };
 
+// Sum of y over the lanes [l - N, l + N] (valid for lanes N .. 31 - N).  Up to
+// N = 2 two shuffles per radius step; wider windows are assembled from
+// power-of-two window sums, e.g. 11 = 8 + 2 + 1 takes 6 shuffles instead of 10.
+template <int N>
+__device__ __forceinline__ float xbox_lanes(float y) {
+    if constexpr (N <= 2) {
+        float x = y;
+#pragma unroll
+        for (int k = 1; k <= N; ++k)
+            x += __shfl_down_sync(0xffffffffu, y, k) + __shfl_up_sync(0xffffffffu, y, k);
+        return x;
+    } else {
+        constexpr int K = 2 * N + 1;
+        float p[5];  // p[j] = sum over lanes l .. l + 2^j - 1
+        p[0] = y;
+#pragma unroll
+        for (int j = 1; j < 5; ++j)
+            p[j] = (1 << j) <= K ? p[j - 1] + __shfl_down_sync(0xffffffffu, p[j - 1], 1 << (j - 1))
+                                 : 0.f;
+        float x = 0.f;
+        int start = -N;  // window start relative to this lane
+#pragma unroll
+        for (int j = 4; j >= 0; --j) {
+            if (K & (1 << j)) {
+                x += start < 0 ? __shfl_up_sync(0xffffffffu, p[j], -start)
+                               : (start == 0 ? p[j] : __shfl_down_sync(0xffffffffu, p[j], start));
+                start += 1 << j;
+            }
+        }
+        return x;
+    }
+}
+
+// Thread = one column (lane) x RY rows; the reference rows sit in registers
+// for all offsets; rows are processed in pairs as packed FP32x2 arithmetic.
 template <int M, int N, typename T, int RY, int NW, int MINB>
 __global__ void __launch_bounds__(32 * NW, MINB)
     nlm2d_fwd_kernel(const __grid_constant__ CUtensorMap tmap, int X, int Y, float inv_scale,
                      float* __restrict__ out, float* __restrict__ zsum, unsigned int* errword) {
     using C = Fwd2d<M, N, T, RY, NW>;
+    static_assert(RY % 2 == 0, "row pairs");
+    constexpr int RP = C::ROWS / 2;
+    constexpr int OP = RY / 2;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* tile = reinterpret_cast<T*>(smem_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF);
@@ -75,38 +113,56 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
 
     const T* aptr = tile + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
-    float num[RY], zs[RY];
+    float2 areg[RP];
 #pragma unroll
-    for (int r = 0; r < RY; ++r) {
-        num[r] = 0.f;
-        zs[r] = 0.f;
-    }
+    for (int rp = 0; rp < RP; ++rp)
+        areg[rp] = make_float2(to_f32(aptr[(2 * rp) * C::BX]), to_f32(aptr[(2 * rp + 1) * C::BX]));
+    float2 zacc[OP], nacc[OP];
+#pragma unroll
+    for (int r = 0; r < OP; ++r) zacc[r] = nacc[r] = make_float2(0.f, 0.f);
+    const float2 minus1 = make_float2(-1.f, -1.f);
 
     for (int oy = -M; oy <= M; ++oy) {
         for (int ox = -M; ox <= M; ++ox) {
             const T* bptr = aptr + oy * C::BX + ox;
             float q[C::ROWS], cand[RY];
 #pragma unroll
-            for (int rr = 0; rr < C::ROWS; ++rr) {
-                const float a = to_f32(aptr[rr * C::BX]);
-                const float b = to_f32(bptr[rr * C::BX]);
-                const float t = a - b;
-                q[rr] = t * t;
-                if (rr >= N && rr < RY + N) cand[rr - N] = b;
+            for (int rp = 0; rp < RP; ++rp) {
+                const float b0 = to_f32(bptr[(2 * rp) * C::BX]);
+                const float b1 = to_f32(bptr[(2 * rp + 1) * C::BX]);
+                const float2 t = __ffma2_rn(make_float2(b0, b1), minus1, areg[rp]);
+                const float2 t2 = __fmul2_rn(t, t);
+                q[2 * rp] = t2.x;
+                q[2 * rp + 1] = t2.y;
+                if (2 * rp >= N && 2 * rp < RY + N) cand[2 * rp - N] = b0;
+                if (2 * rp + 1 >= N && 2 * rp + 1 < RY + N) cand[2 * rp + 1 - N] = b1;
             }
-            float yv = 0.f;
+            float Yv[RY];
+            if constexpr (N == 1) {
 #pragma unroll
-            for (int k = 0; k < C::K; ++k) yv += q[k];
+                for (int r = 0; r < RY; r += 2) {
+                    const float u = q[r + 1] + q[r + 2];
+                    Yv[r] = q[r] + u;
+                    Yv[r + 1] = u + q[r + 3];
+                }
+            } else {
+                float acc = 0.f;
 #pragma unroll
-            for (int r = 0; r < RY; ++r) {
-                if (r > 0) yv = yv + q[r + 2 * N] - q[r - 1];
-                float xv = yv;
+                for (int k = 0; k < C::K; ++k) acc += q[k];
+                Yv[0] = acc;
 #pragma unroll
-                for (int k = 1; k <= N; ++k)
-                    xv += __shfl_down_sync(0xffffffffu, yv, k) + __shfl_up_sync(0xffffffffu, yv, k);
-                const float w = ex2_neg(xv);
-                zs[r] += w;
-                num[r] = fmaf(w, cand[r], num[r]);
+                for (int r = 1; r < RY; ++r) {
+                    acc = acc + q[r + 2 * N] - q[r - 1];
+                    Yv[r] = acc;
+                }
+            }
+#pragma unroll
+            for (int op = 0; op < OP; ++op) {
+                const float x0 = xbox_lanes<N>(Yv[2 * op]);
+                const float x1 = xbox_lanes<N>(Yv[2 * op + 1]);
+                const float2 w = make_float2(ex2_neg(x0), ex2_neg(x1));
+                zacc[op] = __fadd2_rn(zacc[op], w);
+                nacc[op] = __ffma2_rn(w, make_float2(cand[2 * op], cand[2 * op + 1]), nacc[op]);
             }
         }
     }
@@ -118,8 +174,10 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         const int y = Y0 + warp * RY + r;
         if (y >= Y) break;
         const size_t o = (size_t)y * X + x;
-        out[o] = num[r] / zs[r] * inv_scale;
-        if (zsum) zsum[o] = zs[r];
+        const float zs = (r & 1) ? zacc[r / 2].y : zacc[r / 2].x;
+        const float nm = (r & 1) ? nacc[r / 2].y : nacc[r / 2].x;
+        out[o] = nm / zs * inv_scale;
+        if (zsum) zsum[o] = zs;
     }
 }
 
@@ -148,6 +206,29 @@ static cudaError_t run_fwd2d(const Staging& st, const void* staged, float inv_sc
 #define GNLM_FWD2D_CASES(X_) \
     X_(1, 1) X_(3, 1) X_(5, 1) X_(3, 2) X_(5, 2) X_(7, 2) X_(3, 5) X_(7, 5) X_(10, 5)
 
+// Tile variants: 0: 16 rows per thread, 4 warps; 1: 8 rows, 4 warps; 2: 16 rows, 8 warps.
+template <int m, int n>
+static cudaError_t run2d_variant(const Staging& st, const void* staged, bool fp16, int v,
+                                 float inv_scale, float* out, float* zsum, unsigned int* ew,
+                                 cudaStream_t s) {
+    if (fp16) {
+        switch (v) {
+            case 0: return run_fwd2d<m, n, __half, 16, 4, 3>(st, staged, inv_scale, out, zsum, ew, s);
+            case 1: return run_fwd2d<m, n, __half, 8, 4, 4>(st, staged, inv_scale, out, zsum, ew, s);
+            case 2: return run_fwd2d<m, n, __half, 16, 8, 2>(st, staged, inv_scale, out, zsum, ew, s);
+        }
+    } else {
+        switch (v) {
+            case 0: return run_fwd2d<m, n, float, 16, 4, 3>(st, staged, inv_scale, out, zsum, ew, s);
+            case 1: return run_fwd2d<m, n, float, 8, 4, 4>(st, staged, inv_scale, out, zsum, ew, s);
+            case 2: return run_fwd2d<m, n, float, 16, 8, 2>(st, staged, inv_scale, out, zsum, ew, s);
+        }
+    }
+    return cudaErrorInvalidValue;
+}
+
+int nlm2d_fwd_variant_count() { return 3; }
+
 bool nlm2d_fwd_supported(int sr, int pr, bool fp16) {
     (void)fp16;
 #define X_(m, n) \
@@ -158,14 +239,13 @@ bool nlm2d_fwd_supported(int sr, int pr, bool fp16) {
 }
 
 cudaError_t launch_nlm2d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
-                             float inv_scale, float* out, float* zsum, unsigned int* errword,
-                             cudaStream_t stream) {
-#define X_(m, n)                                                                            \
-    if (sr == m && pr == n)                                                                 \
-        return fp16 ? run_fwd2d<m, n, __half, 16, 4, 4>(st, staged, inv_scale, out, zsum,   \
-                                                        errword, stream)                    \
-                    : run_fwd2d<m, n, float, 16, 4, 4>(st, staged, inv_scale, out, zsum,    \
-                                                       errword, stream);
+                             int variant, float inv_scale, float* out, float* zsum,
+                             unsigned int* errword, cudaStream_t stream) {
+    if (variant < 0 || variant >= nlm2d_fwd_variant_count()) return cudaErrorInvalidValue;
+#define X_(m, n)                                                                                \
+    if (sr == m && pr == n)                                                                     \
+        return run2d_variant<m, n>(st, staged, fp16, variant, inv_scale, out, zsum, errword,    \
+                                   stream);
     GNLM_FWD2D_CASES(X_)
 #undef X_
     return cudaErrorNotSupported;

@@ -346,7 +346,8 @@ int nlm2d_forward(const void* d_in, int in_dtype, int X, int Y, int sr, int pr, 
     const float s = weight_scale(pr, 2, h);
     cudaError_t e = launch_stage(d_in, in_dtype, (flags & NLM_FLAG_PREPADDED) != 0, s, st, d_ws, stream);
     if (e != cudaSuccess) return cuda_fail(e, "stage2d launch");
-    e = launch_nlm2d_fwd(st, d_ws, sr, pr, fp16, 1.0f / s, d_out, d_zsum, ew, stream);
+    e = launch_nlm2d_fwd(st, d_ws, sr, pr, fp16, tuned_variant(2, sr, pr, fp16), 1.0f / s, d_out,
+                         d_zsum, ew, stream);
     if (e != cudaSuccess) return cuda_fail(e, "nlm2d_fwd launch");
     return NLM_OK;
 }
@@ -388,7 +389,7 @@ int nlm3d_adjoint(const float* d_in, const float* d_out, const float* d_zsum, co
 
 int nlm_variant_count(int dims, unsigned int flags) {
     if (dims == 3) return nlm3d_fwd_variant_count((flags & NLM_FLAG_FP16_STORAGE) != 0);
-    if (dims == 2) return 1;
+    if (dims == 2) return nlm2d_fwd_variant_count();
     return fail(NLM_ERR_INVALID_ARG, "dims must be 2 or 3");
 }
 
@@ -414,38 +415,39 @@ int nlm_get_variant(int dims, int sr, int pr, unsigned int flags) {
 int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int flags,
                  float* times_ms, nlm_stream_t stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
-    if (dims != 3) {
-        if (dims == 2) return 0;  // one 2D variant
-        return fail(NLM_ERR_INVALID_ARG, "dims must be 2 or 3");
-    }
+    if (dims != 2 && dims != 3) return fail(NLM_ERR_INVALID_ARG, "dims must be 2 or 3");
+    if (dims == 2) Z = 1;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
     int rc = check_dims3(X, Y, Z, sr + pr);
     if (rc) return rc;
-    if (!nlm3d_fwd_supported(sr, pr, fp16))
-        return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
-    const Staging st = staging3d(X, Y, Z, sr + pr, fp16);
+    const bool ok = dims == 3 ? nlm3d_fwd_supported(sr, pr, fp16) : nlm2d_fwd_supported(sr, pr, fp16);
+    if (!ok) return fail(NLM_ERR_UNSUPPORTED, "%dD (sr=%d, pr=%d) not compiled in", dims, sr, pr);
+    const Staging st = dims == 3 ? staging3d(X, Y, Z, sr + pr, fp16)
+                                 : make_staging(X, Y, 1, sr + pr, 0, fp16);
     const size_t nvox = (size_t)X * Y * Z;
     void *d_in = nullptr, *d_ws = nullptr;
     float* d_out = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int best = -1;
     float best_ms = 0.f;
-    const int nv = nlm3d_fwd_variant_count(fp16);
+    const int nv = nlm_variant_count(dims, flags);
     cudaError_t e = cudaMalloc(&d_in, nvox * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, nvox * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&d_ws, st.bytes());
     if (e == cudaSuccess) e = cudaMemsetAsync(d_in, 0, nvox * sizeof(float), stream);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    const float s = weight_scale(pr, 3, 0.05f);
+    const float s = weight_scale(pr, dims, 0.05f);
     if (e == cudaSuccess) e = launch_stage(d_in, NLM_F32, false, s, st, d_ws, stream);
     for (int v = 0; v < nv && e == cudaSuccess; ++v) {
         float ms = 1e30f;
         for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
             e = cudaEventRecord(e0, stream);
             if (e == cudaSuccess)
-                e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, v, 1.0f / s, d_out, nullptr,
-                                     device_error_word(), stream);
+                e = dims == 3 ? launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, v, 1.0f / s, d_out,
+                                                 nullptr, device_error_word(), stream)
+                              : launch_nlm2d_fwd(st, d_ws, sr, pr, fp16, v, 1.0f / s, d_out,
+                                                 nullptr, device_error_word(), stream);
             if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float t = 0.f;
@@ -464,7 +466,7 @@ int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int fla
     cudaFree(d_out);
     cudaFree(d_ws);
     if (e != cudaSuccess) return cuda_fail(e, "nlm_autotune");
-    nlm_set_variant(3, sr, pr, flags, best);
+    nlm_set_variant(dims, sr, pr, flags, best);
     return best;
 }
 

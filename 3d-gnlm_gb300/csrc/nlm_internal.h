@@ -70,9 +70,10 @@ int tuned_variant(int dims, int sr, int pr, bool fp16);
 
 // 2D forward over a staged image (Z = 1, Hz = 0).
 cudaError_t launch_nlm2d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
-                             float inv_scale, float* out, float* zsum, unsigned int* errword,
-                             cudaStream_t stream);
+                             int variant, float inv_scale, float* out, float* zsum,
+                             unsigned int* errword, cudaStream_t stream);
 bool nlm2d_fwd_supported(int sr, int pr, bool fp16);
+int nlm2d_fwd_variant_count();
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
 // dims/strides follow the driver API: dims[0] innermost, strides in bytes for

@@ -83,43 +83,84 @@ static cudaError_t stage_pairs_typed(const void* in, bool prepadded, float scale
     return cudaGetLastError();
 }
 
-// One block per padded row (blockIdx.x = row in [0, Yp), blockIdx.y = plane).
+// Warp per padded row (8 rows per 256-thread block, rows flattened over planes).
+// Each lane writes 16-byte vectors (4 FP32 or 8 FP16 values); columns inside the
+// volume map to the source row directly, only the 2H border columns reflect.
+template <typename Tout>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    static constexpr int N = 4;
+    using T = float4;
+    __device__ static T pack(const float* v) { return make_float4(v[0], v[1], v[2], v[3]); }
+};
+template <>
+struct Vec16<__half> {
+    static constexpr int N = 8;
+    using T = uint4;
+    __device__ static T pack(const float* v) {
+        uint4 r;
+        __half2 h0 = __floats2half2_rn(v[0], v[1]), h1 = __floats2half2_rn(v[2], v[3]);
+        __half2 h2 = __floats2half2_rn(v[4], v[5]), h3 = __floats2half2_rn(v[6], v[7]);
+        r.x = *reinterpret_cast<unsigned int*>(&h0);
+        r.y = *reinterpret_cast<unsigned int*>(&h1);
+        r.z = *reinterpret_cast<unsigned int*>(&h2);
+        r.w = *reinterpret_cast<unsigned int*>(&h3);
+        return r;
+    }
+};
+
 template <typename Tin, typename Tout, bool PREPADDED>
 __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
-                                                    int Z, int H, int Hz, int Xp, int Yp, int Xs,
-                                                    float scale, Tout* __restrict__ dst) {
-    const int py = blockIdx.x;
-    const int pz = blockIdx.y;
-    Tout* drow = dst + ((size_t)pz * Yp + py) * Xs;
+                                                    int Z, int H, int Hz, int Xp, int Yp, int Zp,
+                                                    int Xs, float scale, Tout* __restrict__ dst) {
+    using V = Vec16<Tout>;
+    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= (long long)Yp * Zp) return;
+    const int lane = threadIdx.x & 31;
+    const int py = (int)(row % Yp), pz = (int)(row / Yp);
+    typename V::T* drow = reinterpret_cast<typename V::T*>(dst + row * Xs);
     const Tin* srow;
     if (PREPADDED) {
-        srow = in + ((size_t)pz * Yp + py) * Xp;
+        srow = in + row * Xp;
     } else {
         const int sz = reflect101(pz - Hz, Z);
         const int sy = reflect101(py - H, Y);
         srow = in + ((size_t)sz * Y + sy) * X;
     }
-    for (int px = threadIdx.x; px < Xs; px += blockDim.x) {
-        float v = 0.f;
-        if (px < Xp) {
-            const int sx = PREPADDED ? px : reflect101(px - H, X);
-            v = to_f32(srow[sx]) * scale;
+    for (int c = lane; c * V::N < Xs; c += 32) {
+        float v[V::N];
+#pragma unroll
+        for (int i = 0; i < V::N; ++i) {
+            const int px = c * V::N + i;
+            float x = 0.f;
+            if (px < Xp) {
+                int sx = px;
+                if (!PREPADDED) {
+                    sx = px - H;
+                    if (sx < 0 || sx >= X) sx = reflect101(sx, X);
+                }
+                x = to_f32(srow[sx]) * scale;
+            }
+            v[i] = x;
         }
-        drow[px] = from_f32<Tout>(v);
+        drow[c] = V::pack(v);
     }
 }
 
 template <typename Tin, typename Tout>
 static cudaError_t stage_typed(const void* in, bool prepadded, float scale, const Staging& st,
                                void* dst, cudaStream_t stream) {
-    dim3 grid(st.Yp, st.Zp);
-    const int threads = st.Xs >= 256 ? 256 : (st.Xs >= 128 ? 128 : 64);
+    const long long rows = (long long)st.Yp * st.Zp;
+    const unsigned blocks = (unsigned)((rows + 7) / 8);
     if (prepadded)
-        stage_kernel<Tin, Tout, true><<<grid, threads, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Xs, scale, (Tout*)dst);
+        stage_kernel<Tin, Tout, true><<<blocks, 256, 0, stream>>>(
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Zp, st.Xs, scale,
+            (Tout*)dst);
     else
-        stage_kernel<Tin, Tout, false><<<grid, threads, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Xs, scale, (Tout*)dst);
+        stage_kernel<Tin, Tout, false><<<blocks, 256, 0, stream>>>(
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Zp, st.Xs, scale,
+            (Tout*)dst);
     return cudaGetLastError();
 }
 

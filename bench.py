@@ -209,6 +209,30 @@ def bench_batched(torch, gnlm, reps=3):
             "max_abs_diff_vs_sequential": same}
 
 
+def bench_2d(torch, gnlm, reps=5):
+    """2048^2 image (32 discs/rectangles, sigma 0.08), search 11^2, patch 5^2, h 0.08."""
+    from gnlm import phantom
+    im, _ = phantom.disc_rect_phantom((2048, 2048), n_shapes=32, sigma=0.08, seed=0)
+    x = torch.from_numpy(im).cuda()
+    best, tune = gnlm.autotune(2, (1, 2048, 2048), 5, 2)
+    out = torch.empty_like(x)
+    gnlm.nlm2d_forward(x, 5, 2, 0.08, out=out)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        gnlm.nlm2d_forward(x, 5, 2, 0.08, out=out)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = min(ms)
+    return {"shape": [2048, 2048], "search_radius": 5, "patch_radius": 2, "ms": round(t, 4),
+            "value": round(2048 * 2048 / (t * 1e-3) / 1e6, 1), "unit": "Mpixel/s",
+            "tflops": round(10 * 121 * 2048 * 2048 / (t * 1e-3) / 1e12, 2), "variant": best,
+            "autotune_ms": [round(v, 4) for v in tune]}
+
+
 def bench_adjoint(torch, gnlm, steps=50):
     """128^3 (ellipsoids, sigma 0.05, sr 3, pr 1): forward + adjoint per step, used
     to fit h by gradient descent on the MSE to the clean phantom."""
@@ -404,6 +428,7 @@ def run_gnlm(args):
     peak_x2 = fp32_peak_tflops(torch, packed=True)
     batched = bench_batched(torch, gnlm) if not args.skip_extra else None
     adjoint = bench_adjoint(torch, gnlm) if not args.skip_extra else None
+    image2d = bench_2d(torch, gnlm) if not args.skip_extra else None
     fused_mean = statistics.mean(fused_ms)
     achieved = FLOPS_PER_PAIR * OFFSETS * nvox / (fused_mean * 1e-3) / 1e12
     traffic = read_profile_traffic("nlm3d_fwd_kernel")
@@ -436,6 +461,7 @@ def run_gnlm(args):
                   "fp16_storage": {"value": round(fp16_value, 2), "max_abs_err_vs_fp64": err16},
                   "batched": batched},
         "adjoint": adjoint,
+        "nlm2d": image2d,
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:

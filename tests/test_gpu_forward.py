@@ -225,3 +225,21 @@ def test_autotune_records_a_variant(torch_cuda, gnlm_lib):
     assert times[best] == min(times)
     gnlm_lib.set_variant(3, 3, 1, -1)
     assert gnlm_lib.get_variant(3, 3, 1) == 0
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+def test_2d_every_tile_variant(torch_cuda, gnlm_lib, fp16):
+    tol = TOL_F16 if fp16 else TOL_F32
+    for shape, sr, pr in [((61, 90), 5, 2), ((40, 33), 10, 5), ((37, 70), 3, 1), ((29, 64), 7, 2)]:
+        im, _ = phantom.disc_rect_phantom(shape, n_shapes=6, sigma=0.08, seed=sum(shape) + pr)
+        o = O.nlm2d(im, sr, pr, 0.08, dtype=np.float64)
+        try:
+            for var in range(gnlm_lib.variant_count(2, fp16)):
+                gnlm_lib.set_variant(2, sr, pr, var, fp16)
+                g = _gpu2d(torch_cuda, gnlm_lib, im, sr, pr, 0.08, fp16_storage=fp16)
+                assert np.abs(g - o).max() <= tol, (shape, sr, pr, var)
+        finally:
+            gnlm_lib.set_variant(2, sr, pr, -1, fp16)
+    best, times = gnlm_lib.autotune(2, (1, 128, 256), 5, 2)
+    assert 0 <= best < len(times) and times[best] == min(times)
+    gnlm_lib.set_variant(2, 5, 2, -1)
