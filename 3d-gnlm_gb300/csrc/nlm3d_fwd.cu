@@ -11,7 +11,7 @@ template <int M, int N, typename T, int RY, int RZ, int NW, int MINB, bool AREG,
 __global__ void __launch_bounds__(32 * NW, MINB)
     nlm3d_fwd_kernel(const __grid_constant__ CUtensorMap tmap, int X, int Y, int Z,
                      float inv_scale, float* __restrict__ out, float* __restrict__ zsum,
-                     unsigned int* errword) {
+                     unsigned int* errword, int bz0) {
     using C = Fwd3d<M, N, T, RY, RZ, NW>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* tile = reinterpret_cast<T*>(smem_raw);
@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
     __syncthreads();
     fwd3d_tile<M, N, T, RY, RZ, NW, AREG, KAHAN>(&tmap, tile, bar, 0, blockIdx.x, blockIdx.y,
-                                                  blockIdx.z, X, Y, Z, inv_scale, out, zsum,
+                                                  blockIdx.z + bz0, X, Y, Z, inv_scale, out, zsum,
                                                   errword);
 }
 
@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     nlm3d_fwd_h2_kernel(const __grid_constant__ CUtensorMap mapE,
                         const __grid_constant__ CUtensorMap mapO, int X, int Y, int Z,
                         float inv_scale, float* __restrict__ out, float* __restrict__ zsum,
-                        unsigned int* errword) {
+                        unsigned int* errword, int bz0) {
     using C = Fwd3dH2<M, N, RY, RZ, NW>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF);
@@ -42,14 +42,14 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
     __syncthreads();
     fwd3d_tile_h2<M, N, RY, RZ, NW, KAHAN>(&mapE, &mapO, smem_raw, bar, 0, blockIdx.x,
-                                           blockIdx.y, blockIdx.z, X, Y, Z, inv_scale, out, zsum,
+                                           blockIdx.y, blockIdx.z + bz0, X, Y, Z, inv_scale, out, zsum,
                                            errword);
 }
 
 template <int M, int N, int RY, int RZ, int NW, int MINB, bool KAHAN>
 static cudaError_t run_fwd3d_h2(const Staging& st, const void* staged, float inv_scale,
                                 float* out, float* zsum, unsigned int* errword,
-                                cudaStream_t stream) {
+                                cudaStream_t stream, int zt0, int zt1) {
     using C = Fwd3dH2<M, N, RY, RZ, NW>;
     CUtensorMap mapE, mapO;
     const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yq, (uint64_t)st.Zp};
@@ -63,15 +63,18 @@ static cudaError_t run_fwd3d_h2(const Staging& st, const void* staged, float inv
     auto kern = nlm3d_fwd_h2_kernel<M, N, RY, RZ, NW, MINB, KAHAN>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY, (st.Z + RZ - 1) / RZ);
+    if (zt1 < 0) zt1 = (st.Z + RZ - 1) / RZ;
+    if (zt1 <= zt0) return cudaSuccess;
+    dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY, zt1 - zt0);
     kern<<<grid, 32 * NW, C::SMEM_BYTES, stream>>>(mapE, mapO, st.X, st.Y, st.Z, inv_scale, out,
-                                                   zsum, errword);
+                                                   zsum, errword, zt0);
     return cudaGetLastError();
 }
 
 template <int M, int N, typename T, int RY, int RZ, int NW, int MINB, bool AREG, bool KAHAN>
 static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_scale, float* out,
-                             float* zsum, unsigned int* errword, cudaStream_t stream) {
+                             float* zsum, unsigned int* errword, cudaStream_t stream, int zt0,
+                             int zt1) {
     using C = Fwd3d<M, N, T, RY, RZ, NW>;
     CUtensorMap map;
     const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
@@ -83,9 +86,11 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
     auto kern = nlm3d_fwd_kernel<M, N, T, RY, RZ, NW, MINB, AREG, KAHAN>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY, (st.Z + RZ - 1) / RZ);
+    if (zt1 < 0) zt1 = (st.Z + RZ - 1) / RZ;
+    if (zt1 <= zt0) return cudaSuccess;
+    dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY, zt1 - zt0);
     kern<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(map, st.X, st.Y, st.Z, inv_scale, out, zsum,
-                                                      errword);
+                                                      errword, zt0);
     return cudaGetLastError();
 }
 
@@ -103,25 +108,31 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
 template <int m, int n>
 static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16, int v,
                                float inv_scale, float* out, float* zsum, unsigned int* ew,
-                               cudaStream_t s) {
+                               cudaStream_t s, int zt0, int zt1) {
     if (!fp16) {
         switch (v) {
-            case 0: return run_fwd3d<m, n, float, 4, 8, 4, 2, true, false>(st, staged, inv_scale, out, zsum, ew, s);
-            case 1: return run_fwd3d<m, n, float, 4, 8, 4, 3, false, false>(st, staged, inv_scale, out, zsum, ew, s);
-            case 2: return run_fwd3d<m, n, float, 4, 4, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s);
-            case 3: return run_fwd3d<m, n, float, 2, 8, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s);
+            case 0: return run_fwd3d<m, n, float, 4, 8, 4, 2, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 1: return run_fwd3d<m, n, float, 4, 8, 4, 3, false, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 2: return run_fwd3d<m, n, float, 4, 4, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 3: return run_fwd3d<m, n, float, 2, 8, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
         }
     } else {
         switch (v) {
-            case 0: return run_fwd3d_h2<m, n, 4, 6, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s);
-            case 1: return run_fwd3d_h2<m, n, 4, 8, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s);
-            case 2: return run_fwd3d_h2<m, n, 2, 8, 4, 3, true>(st, staged, inv_scale, out, zsum, ew, s);
+            case 0: return run_fwd3d_h2<m, n, 4, 6, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 1: return run_fwd3d_h2<m, n, 4, 8, 4, 2, true>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 2: return run_fwd3d_h2<m, n, 2, 8, 4, 3, true>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
         }
     }
     return cudaErrorInvalidValue;
 }
 
 int nlm3d_fwd_variant_count(bool fp16) { return fp16 ? 3 : 4; }
+
+int nlm3d_fwd_tile_z(bool fp16, int v) {
+    static const int f32[4] = {8, 8, 4, 8}, f16[3] = {6, 8, 8};
+    if (v < 0 || v >= nlm3d_fwd_variant_count(fp16)) return 0;
+    return fp16 ? f16[v] : f32[v];
+}
 
 bool nlm3d_fwd_supported(int sr, int pr, bool fp16) {
     (void)fp16;
@@ -134,11 +145,12 @@ bool nlm3d_fwd_supported(int sr, int pr, bool fp16) {
 
 cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
                              int variant, float inv_scale, float* out, float* zsum,
-                             unsigned int* errword, cudaStream_t stream) {
+                             unsigned int* errword, cudaStream_t stream, int zt0, int zt1) {
     if (variant < 0 || variant >= nlm3d_fwd_variant_count(fp16)) return cudaErrorInvalidValue;
 #define X_(m, n)                                                                                \
     if (sr == m && pr == n)                                                                     \
-        return run_variant<m, n>(st, staged, fp16, variant, inv_scale, out, zsum, errword, stream);
+        return run_variant<m, n>(st, staged, fp16, variant, inv_scale, out, zsum, errword, stream, \
+                                 zt0, zt1);
     GNLM_FWD3D_CASES(X_)
 #undef X_
     return cudaErrorNotSupported;

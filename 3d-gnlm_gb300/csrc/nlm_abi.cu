@@ -6,7 +6,9 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
+#include <vector>
 #include <mutex>
 #include <utility>
 
@@ -42,7 +44,9 @@ std::map<int, unsigned int*> g_errword;                    // device -> error wo
 std::map<std::pair<int, cudaStream_t>, std::pair<void*, size_t>> g_ws;  // cached workspaces
 
 struct HostPath {
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // staging + compute
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+    std::vector<cudaEvent_t> ev_in, ev_out;
     void* d_in = nullptr;
     size_t in_bytes = 0;
     float* d_out = nullptr;
@@ -477,6 +481,81 @@ static HostPath* host_path(int dev) {
     return hp;
 }
 
+static int ensure_events(std::vector<cudaEvent_t>& v, size_t n) {
+    while (v.size() < n) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        if (r != cudaSuccess) return cuda_fail(r, "cudaEventCreate");
+        v.push_back(e);
+    }
+    return NLM_OK;
+}
+
+// 3D host path pipelined over z chunks: the host->device copy of later input
+// chunks and the device->host copy of finished output chunks overlap the staging
+// and NLM kernels of the current chunk.  Output chunk k = planes [k CZ, (k+1) CZ),
+// CZ a multiple of the kernel's z tile; it waits only for the input planes its
+// REFLECT_101 halo reaches.  Returns 1 when the volume is too thin to split.
+static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype, int X, int Y,
+                                    int Z, int sr, int pr, float h, float* h_out,
+                                    unsigned int flags) {
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    const bool prepadded = (flags & NLM_FLAG_PREPADDED) != 0;
+    const int H = sr + pr;
+    const int variant = tuned_variant(3, sr, pr, fp16);
+    const int RZ = nlm3d_fwd_tile_z(fp16, variant);
+    if (RZ <= 0) return 1;
+    const int CZ = std::max(1, (Z / 8 + RZ - 1) / RZ) * RZ;
+    const int nch = (Z + CZ - 1) / CZ;
+    if (nch < 2) return 1;
+    cudaError_t e = cudaSuccess;
+    if (!hp->s_h2d) e = cudaStreamCreateWithFlags(&hp->s_h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !hp->s_d2h) e = cudaStreamCreateWithFlags(&hp->s_d2h, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    const Staging st = staging3d(X, Y, Z, H, fp16);
+    const size_t plane_in =
+        (prepadded ? (size_t)(X + 2 * H) * (Y + 2 * H) : (size_t)X * Y) * dtype_bytes(in_dtype);
+    const int in_planes = prepadded ? Z + 2 * H : Z;
+    const int nin = (in_planes + CZ - 1) / CZ;
+    int rc = ensure_events(hp->ev_in, nin);
+    if (rc == NLM_OK) rc = ensure_events(hp->ev_out, nch);
+    if (rc != NLM_OK) return rc;
+    const char* src = static_cast<const char*>(h_in);
+    char* din = static_cast<char*>(hp->d_in);
+    for (int j = 0; j < nin; ++j) {
+        const size_t p0 = (size_t)j * CZ, p1 = std::min((size_t)in_planes, p0 + CZ);
+        e = cudaMemcpyAsync(din + p0 * plane_in, src + p0 * plane_in, (p1 - p0) * plane_in,
+                            cudaMemcpyHostToDevice, hp->s_h2d);
+        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_in[j], hp->s_h2d);
+        if (e != cudaSuccess) return cuda_fail(e, "host->device chunk copy");
+    }
+    const float s = weight_scale(pr, 3, h);
+    unsigned int* ew = device_error_word();
+    const size_t plane_out = (size_t)X * Y;
+    for (int k = 0; k < nch; ++k) {
+        const int z0 = k * CZ, z1 = std::min(Z, z0 + CZ);
+        const int p0 = k == 0 ? 0 : z0 + 2 * H, p1 = z1 + 2 * H;  // new padded planes
+        const int need = prepadded ? p1 - 1 : std::min(Z, z1 + H) - 1;  // last input plane read
+        const int j = std::min(nin - 1, need / CZ);
+        e = cudaStreamWaitEvent(hp->stream, hp->ev_in[j], 0);
+        if (e == cudaSuccess) e = launch_stage(hp->d_in, in_dtype, prepadded, s, st, hp->d_ws, hp->stream, p0, p1);
+        if (e == cudaSuccess)
+            e = launch_nlm3d_fwd(st, hp->d_ws, sr, pr, fp16, variant, 1.0f / s, hp->d_out, nullptr,
+                                 ew, hp->stream, z0 / RZ, (z1 + RZ - 1) / RZ);
+        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_out[k], hp->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(hp->s_d2h, hp->ev_out[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h_out + (size_t)z0 * plane_out, hp->d_out + (size_t)z0 * plane_out,
+                                (size_t)(z1 - z0) * plane_out * sizeof(float),
+                                cudaMemcpyDeviceToHost, hp->s_d2h);
+        if (e != cudaSuccess) return cuda_fail(e, "pipelined forward");
+    }
+    e = cudaStreamSynchronize(hp->s_d2h);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(hp->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    return NLM_OK;
+}
+
 static int host_forward(const void* h_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
                         float h, float* h_out, unsigned int flags, int dims) {
     int rc = check_common(h_in, h_out, in_dtype, sr, pr, h, flags);
@@ -503,6 +582,10 @@ static int host_forward(const void* h_in, int in_dtype, int X, int Y, int Z, int
     if ((rc = ensure_buffer(&hp->d_in, &hp->in_bytes, in_bytes, hp->stream))) return rc;
     if ((rc = ensure_buffer((void**)&hp->d_out, &hp->out_bytes, out_bytes, hp->stream))) return rc;
     if ((rc = ensure_buffer(&hp->d_ws, &hp->ws_bytes, ws, hp->stream))) return rc;
+    if (dims == 3 && nlm3d_fwd_supported(sr, pr, (flags & NLM_FLAG_FP16_STORAGE) != 0)) {
+        rc = host_forward3d_pipelined(hp, h_in, in_dtype, X, Y, Z, sr, pr, h, h_out, flags);
+        if (rc != 1) return rc;
+    }
     e = cudaMemcpyAsync(hp->d_in, h_in, in_bytes, cudaMemcpyHostToDevice, hp->stream);
     if (e != cudaSuccess) return cuda_fail(e, "host->device copy");
     rc = dims == 3 ? nlm3d_forward(hp->d_in, in_dtype, X, Y, Z, sr, pr, h, hp->d_out, nullptr,

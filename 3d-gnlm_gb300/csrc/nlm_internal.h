@@ -44,16 +44,22 @@ Staging make_staging_pairs(int X, int Y, int Z, int H);
 // Pads, converts and scales `in` into `dst` (layout of `st`).  in_dtype is an
 // nlm_dtype; with `prepadded` the input already has the halo (layout
 // [Zp][Yp][Xp], no stride padding) and is copied, converted and scaled only.
+// [pz0, pz1): range of padded planes to stage (pz1 < 0: through the last).
 cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float scale,
-                         const Staging& st, void* dst, cudaStream_t stream);
+                         const Staging& st, void* dst, cudaStream_t stream, int pz0 = 0,
+                         int pz1 = -1);
 
 // 3D forward over a staged volume.  Returns cudaErrorNotSupported when the
 // (sr, pr, fp16) combination has no compiled instance.
+// [zt0, zt1): range of z tiles to compute (zt1 < 0: through the last); a z tile
+// is nlm3d_fwd_tile_z(fp16, variant) output planes.
 cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
                              int variant, float inv_scale, float* out, float* zsum,
-                             unsigned int* errword, cudaStream_t stream);
+                             unsigned int* errword, cudaStream_t stream, int zt0 = 0,
+                             int zt1 = -1);
 bool nlm3d_fwd_supported(int sr, int pr, bool fp16);
 int nlm3d_fwd_variant_count(bool fp16);
+int nlm3d_fwd_tile_z(bool fp16, int variant);
 
 // 3D adjoint (see nlm3d_adj.cu).  Scratch: G, out', gpad' (each st.bytes()) and
 // adj3d_ctas() doubles of h partial sums.

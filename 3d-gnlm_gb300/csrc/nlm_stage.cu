@@ -43,8 +43,8 @@ template <typename Tin, bool PREPADDED>
 __global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict__ in, int X, int Y,
                                                           int Z, int H, int Xp, int Yp, int Xs,
                                                           int Yq, size_t copy_elems, float scale,
-                                                          __half2* __restrict__ dst) {
-    const int k = blockIdx.x, pz = blockIdx.y, c = blockIdx.z;
+                                                          __half2* __restrict__ dst, int pz0) {
+    const int k = blockIdx.x, pz = blockIdx.y + pz0, c = blockIdx.z;
     const int r0 = 2 * k + c, r1 = r0 + 1;
     __half2* drow = dst + c * copy_elems + ((size_t)pz * Yq + k) * Xs;
     const Tin *s0 = nullptr, *s1 = nullptr;
@@ -69,17 +69,17 @@ __global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict_
 
 template <typename Tin>
 static cudaError_t stage_pairs_typed(const void* in, bool prepadded, float scale, const Staging& st,
-                                     void* dst, cudaStream_t stream) {
-    dim3 grid(st.Yq, st.Zp, 2);
+                                     void* dst, cudaStream_t stream, int pz0, int pz1) {
+    dim3 grid(st.Yq, pz1 - pz0, 2);
     const size_t copy_elems = st.copy_bytes() / 4;
     if (prepadded)
         stage_pairs_kernel<Tin, true><<<grid, 256, 0, stream>>>(
             (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp, st.Yp, st.Xs, st.Yq, copy_elems, scale,
-            (__half2*)dst);
+            (__half2*)dst, pz0);
     else
         stage_pairs_kernel<Tin, false><<<grid, 256, 0, stream>>>(
             (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp, st.Yp, st.Xs, st.Yq, copy_elems, scale,
-            (__half2*)dst);
+            (__half2*)dst, pz0);
     return cudaGetLastError();
 }
 
@@ -112,11 +112,12 @@ struct Vec16<__half> {
 
 template <typename Tin, typename Tout, bool PREPADDED>
 __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
-                                                    int Z, int H, int Hz, int Xp, int Yp, int Zp,
-                                                    int Xs, float scale, Tout* __restrict__ dst) {
+                                                    int Z, int H, int Hz, int Xp, int Yp,
+                                                    long long row0, long long row1, int Xs,
+                                                    float scale, Tout* __restrict__ dst) {
     using V = Vec16<Tout>;
-    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (row >= (long long)Yp * Zp) return;
+    const long long row = row0 + (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= row1) return;
     const int lane = threadIdx.x & 31;
     const int py = (int)(row % Yp), pz = (int)(row / Yp);
     typename V::T* drow = reinterpret_cast<typename V::T*>(dst + row * Xs);
@@ -150,41 +151,44 @@ __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, 
 
 template <typename Tin, typename Tout>
 static cudaError_t stage_typed(const void* in, bool prepadded, float scale, const Staging& st,
-                               void* dst, cudaStream_t stream) {
-    const long long rows = (long long)st.Yp * st.Zp;
-    const unsigned blocks = (unsigned)((rows + 7) / 8);
+                               void* dst, cudaStream_t stream, int pz0, int pz1) {
+    const long long row0 = (long long)st.Yp * pz0, row1 = (long long)st.Yp * pz1;
+    const unsigned blocks = (unsigned)((row1 - row0 + 7) / 8);
     if (prepadded)
         stage_kernel<Tin, Tout, true><<<blocks, 256, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Zp, st.Xs, scale,
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, row0, row1, st.Xs, scale,
             (Tout*)dst);
     else
         stage_kernel<Tin, Tout, false><<<blocks, 256, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, st.Zp, st.Xs, scale,
+            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, row0, row1, st.Xs, scale,
             (Tout*)dst);
     return cudaGetLastError();
 }
 
 cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float scale,
-                         const Staging& st, void* dst, cudaStream_t stream) {
+                         const Staging& st, void* dst, cudaStream_t stream, int pz0, int pz1) {
+    if (pz1 < 0 || pz1 > st.Zp) pz1 = st.Zp;
+    if (pz0 < 0) pz0 = 0;
+    if (pz1 <= pz0) return cudaSuccess;
     if (st.pairs) {
         switch (in_dtype) {
-            case NLM_U8: return stage_pairs_typed<unsigned char>(in, prepadded, scale, st, dst, stream);
-            case NLM_F16: return stage_pairs_typed<__half>(in, prepadded, scale, st, dst, stream);
-            case NLM_F32: return stage_pairs_typed<float>(in, prepadded, scale, st, dst, stream);
+            case NLM_U8: return stage_pairs_typed<unsigned char>(in, prepadded, scale, st, dst, stream, pz0, pz1);
+            case NLM_F16: return stage_pairs_typed<__half>(in, prepadded, scale, st, dst, stream, pz0, pz1);
+            case NLM_F32: return stage_pairs_typed<float>(in, prepadded, scale, st, dst, stream, pz0, pz1);
             default: return cudaErrorInvalidValue;
         }
     }
     const bool fp16 = st.elem == 2;
     switch (in_dtype) {
         case NLM_U8:
-            return fp16 ? stage_typed<unsigned char, __half>(in, prepadded, scale, st, dst, stream)
-                        : stage_typed<unsigned char, float>(in, prepadded, scale, st, dst, stream);
+            return fp16 ? stage_typed<unsigned char, __half>(in, prepadded, scale, st, dst, stream, pz0, pz1)
+                        : stage_typed<unsigned char, float>(in, prepadded, scale, st, dst, stream, pz0, pz1);
         case NLM_F16:
-            return fp16 ? stage_typed<__half, __half>(in, prepadded, scale, st, dst, stream)
-                        : stage_typed<__half, float>(in, prepadded, scale, st, dst, stream);
+            return fp16 ? stage_typed<__half, __half>(in, prepadded, scale, st, dst, stream, pz0, pz1)
+                        : stage_typed<__half, float>(in, prepadded, scale, st, dst, stream, pz0, pz1);
         case NLM_F32:
-            return fp16 ? stage_typed<float, __half>(in, prepadded, scale, st, dst, stream)
-                        : stage_typed<float, float>(in, prepadded, scale, st, dst, stream);
+            return fp16 ? stage_typed<float, __half>(in, prepadded, scale, st, dst, stream, pz0, pz1)
+                        : stage_typed<float, float>(in, prepadded, scale, st, dst, stream, pz0, pz1);
         default:
             return cudaErrorInvalidValue;
     }

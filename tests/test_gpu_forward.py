@@ -243,3 +243,25 @@ def test_2d_every_tile_variant(torch_cuda, gnlm_lib, fp16):
     best, times = gnlm_lib.autotune(2, (1, 128, 256), 5, 2)
     assert 0 <= best < len(times) and times[best] == min(times)
     gnlm_lib.set_variant(2, 5, 2, -1)
+
+
+@pytest.mark.parametrize("shape,sr,pr,fp16,u8_prepadded", [
+    ((37, 30, 50), 3, 1, False, False), ((64, 20, 33), 5, 1, False, False),
+    ((41, 28, 40), 3, 1, True, False), ((33, 24, 31), 3, 2, False, False),
+    ((48, 36, 40), 3, 1, False, True)])
+def test_3d_pipelined_host_path_matches_device_path(torch_cuda, gnlm_lib, shape, sr, pr, fp16,
+                                                    u8_prepadded):
+    """The host-buffer call overlaps its copies with compute over z chunks; the
+    result must equal the device-buffer call exactly."""
+    torch = torch_cuda
+    v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=6, sigma=0.05, seed=sum(shape) + sr)
+    h = 0.05
+    if u8_prepadded:
+        v = np.ascontiguousarray(O.pad_reflect101(np.clip(v * 255, 0, 255).astype(np.uint8), sr + pr))
+        h = 10.0
+    dev = gnlm_lib.nlm3d_forward(torch.from_numpy(v).cuda(), sr, pr, h, fp16_storage=fp16,
+                                 prepadded=u8_prepadded, shape=shape).cpu().numpy()
+    pinned = torch.from_numpy(v).pin_memory().numpy()
+    host = gnlm_lib.nlm3d_forward_host(pinned, sr, pr, h, fp16_storage=fp16,
+                                       prepadded=u8_prepadded, shape=shape)
+    assert np.array_equal(dev, host)
