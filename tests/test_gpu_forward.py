@@ -112,7 +112,8 @@ def test_3d_host_path_and_workspace_forms_agree(torch_cuda, gnlm_lib):
         c = gnlm_lib.nlm3d_forward(x, 3, 1, 0.05, workspace=ws, stream=s)
     s.synchronize()
     assert np.array_equal(a, c.cpu().numpy())
-    too_small = torch.empty(nbytes - 256, dtype=torch.uint8, device="cuda")
+    # the query covers every tile variant's layout; a quarter of it fits none
+    too_small = torch.empty(nbytes // 4 // 256 * 256, dtype=torch.uint8, device="cuda")
     with pytest.raises(gnlm_lib.NLMError) as ei:
         gnlm_lib.nlm3d_forward(x, 3, 1, 0.05, workspace=too_small)
     assert ei.value.code == gnlm_lib.NLM_ERR_WORKSPACE
