@@ -128,19 +128,34 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
 
 int nlm3d_fwd_variant_count(bool fp16) { return fp16 ? 3 : 4; }
 
-int nlm3d_fwd_tile_z(bool fp16, int v) {
-    static const int f32[4] = {8, 8, 4, 8}, f16[3] = {6, 8, 8};
-    if (v < 0 || v >= nlm3d_fwd_variant_count(fp16)) return 0;
-    return fp16 ? f16[v] : f32[v];
-}
-
-bool nlm3d_fwd_supported(int sr, int pr, bool fp16) {
-    (void)fp16;
+static bool small_case(int sr, int pr) {
 #define X_(m, n) \
     if (sr == m && pr == n) return true;
     GNLM_FWD3D_CASES(X_)
 #undef X_
     return false;
+}
+
+// Pairs without a register-brick instance run on the large-patch kernel (FP32
+// staging only).
+bool nlm3d_fwd_large_patch(int sr, int pr, bool fp16) {
+    return !fp16 && !small_case(sr, pr) && nlm3d_lp_supported(sr, pr);
+}
+
+size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16) {
+    if (!nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
+    return align_up((size_t)X * Y * Z * sizeof(float2), kAlign);
+}
+
+int nlm3d_fwd_tile_z(int sr, int pr, bool fp16, int v) {
+    static const int f32[4] = {8, 8, 4, 8}, f16[3] = {6, 8, 8};
+    if (v < 0 || v >= nlm3d_fwd_variant_count(fp16)) return 0;
+    if (nlm3d_fwd_large_patch(sr, pr, fp16)) return nlm3d_lp_tile_z(v);
+    return fp16 ? f16[v] : f32[v];
+}
+
+bool nlm3d_fwd_supported(int sr, int pr, bool fp16) {
+    return small_case(sr, pr) || nlm3d_fwd_large_patch(sr, pr, fp16);
 }
 
 cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
@@ -153,6 +168,12 @@ cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int 
                                  zt0, zt1);
     GNLM_FWD3D_CASES(X_)
 #undef X_
+    if (nlm3d_fwd_large_patch(sr, pr, fp16)) {
+        float2* acc = reinterpret_cast<float2*>(static_cast<char*>(const_cast<void*>(staged)) +
+                                                st.bytes());
+        return launch_nlm3d_lp(st, staged, sr, pr, variant, inv_scale, out, zsum, acc, errword,
+                               stream, zt0, zt1);
+    }
     return cudaErrorNotSupported;
 }
 

@@ -258,7 +258,8 @@ int nlm_release_cached(void) {
 size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags) {
     if (X < 1 || Y < 1 || Z < 1 || sr < 0 || pr < 0) return 0;
     const int H = sr + pr;
-    return staging3d(X, Y, Z, H, (flags & NLM_FLAG_FP16_STORAGE) != 0).bytes();
+    const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
+    return staging3d(X, Y, Z, H, fp16).bytes() + nlm3d_fwd_extra_bytes(X, Y, Z, sr, pr, fp16);
 }
 
 static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
@@ -269,7 +270,7 @@ static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int
     if (!nlm3d_fwd_supported(sr, pr, fp16))
         return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
     Staging st = staging3d(X, Y, Z, H, fp16);
-    int rc = resolve_ws(d_ws, ws_bytes, st.bytes(), stream);
+    int rc = resolve_ws(d_ws, ws_bytes, nlm3d_workspace_bytes(X, Y, Z, sr, pr, flags), stream);
     if (rc) return rc;
     cudaError_t e = launch_stage(d_in, in_dtype, (flags & NLM_FLAG_PREPADDED) != 0,
                                  weight_scale(pr, 3, h), st, *d_ws, stream);
@@ -437,7 +438,8 @@ int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int fla
     const int nv = nlm_variant_count(dims, flags);
     cudaError_t e = cudaMalloc(&d_in, nvox * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, nvox * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&d_ws, st.bytes());
+    const size_t ws_need = dims == 3 ? nlm3d_workspace_bytes(X, Y, Z, sr, pr, flags) : st.bytes();
+    if (e == cudaSuccess) e = cudaMalloc(&d_ws, ws_need);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_in, 0, nvox * sizeof(float), stream);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -503,7 +505,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const bool prepadded = (flags & NLM_FLAG_PREPADDED) != 0;
     const int H = sr + pr;
     const int variant = tuned_variant(3, sr, pr, fp16);
-    const int RZ = nlm3d_fwd_tile_z(fp16, variant);
+    const int RZ = nlm3d_fwd_tile_z(sr, pr, fp16, variant);
     if (RZ <= 0) return 1;
     const int CZ = std::max(1, (Z / 8 + RZ - 1) / RZ) * RZ;
     const int nch = (Z + CZ - 1) / CZ;
