@@ -12,10 +12,11 @@
 // offsets and streams the chunk's planes (plus the patch halo) in z:
 //   A  each thread owns 4 halo columns of one halo row and keeps, per x offset,
 //      the running z-sum Sz of squared differences over the 2pr+1 planes around
-//      the current plane (add the entering plane, subtract the leaving one);
-//      the reference plane and the candidate plane of a step come in as TMA
-//      boxes (double-buffered, prefetched one step ahead), and one 4-column
-//      candidate window serves all 2sr+1 x offsets;
+//      the current plane (add the entering plane, subtract the leaving one; the
+//      first window is built two planes per step); the reference plane and the
+//      candidate plane of a step come in as TMA boxes (double-buffered,
+//      prefetched one step ahead), and one 4-column candidate window serves all
+//      2sr+1 x offsets;
 //   B  x box sum of Sz along each halo row (shared memory, running sum);
 //   C  y box sum down each output column, in place (running sum) -> D;
 //   D  w = 2^(-D) (the staging pass pre-scaled the volume so D is the base-2
@@ -51,7 +52,7 @@ struct Lp3d {
     static constexpr int PSZ = (BWR % 8 == 4) ? BWR : BWR + 4;  // Sz row pitch, PSZ/4 odd
     static constexpr int PSX = 36;             // Sx row pitch (32 used), PSX/4 odd
     static constexpr int THREADS = 512;
-    static constexpr int NA = NG * HY;         // stage A items (one per thread)
+    static constexpr int NA = 16 * HY;         // stage A threads (16 per halo row, NG used)
     static constexpr int NB = K * HY;          // stage B items (k, halo row)
     static constexpr int NC = K * CX;          // stage C items (k, column)
     static constexpr int REF_TX = BWR * HY * 4;    // bytes of a reference plane box
@@ -66,7 +67,9 @@ struct Lp3d {
     static constexpr int BAR_OFF = D_OFF + 2 * CAND_SLOT;
     static constexpr int SMEM_BYTES = BAR_OFF + 64;
     static_assert(M >= 1 && N >= 1, "radii");
-    static_assert(NA <= THREADS && NB <= THREADS && NC <= THREADS, "one item per thread");
+    static_assert(NG <= 16 && NA <= THREADS && NB <= THREADS && NC <= THREADS,
+                  "one item per thread");
+    static_assert(CX == 32 && CY == 16, "stage B/C split outputs into two runs");
     static_assert(CX * CY == THREADS, "one stage-D voxel per thread");
     static_assert(4 * R >= M, "candidate window covers the x offsets");
     static_assert(BWR >= MA + HX, "Sz row covers the halo");
@@ -104,29 +107,40 @@ __global__ void __launch_bounds__(512, 1)
     const int Z0 = (blockIdx.z + a.zc0) * a.TZ;
     const int TZc = min(a.TZ, a.Z - Z0);
     if (TZc <= 0) return;  // uniform over the CTA
-    const int SPP = TZc + 2 * N;            // steps per pass
-    const int P = C::K * C::K;              // passes
-    const int T = P * SPP;                  // steps
-    const int TD = P * TZc;                 // steps with output (stage B..D)
+    // A pass is N warm-up steps, each adding two planes of the first window
+    // (padded planes Z0+M .. Z0+M+2N-1), then TZc output steps: output plane
+    // Z0+q adds padded plane Z0+M+2N+q and, for q >= 1, drops Z0+M+q-1.
+    const int SPP = N + TZc;
+    const int P = C::K * C::K;  // passes
+    const int T = P * SPP;      // steps
+    const int TD = P * TZc;     // output steps
 
     auto abuf = [&](int b) { return smem + C::A_OFF + b * C::ABUF; };
     auto dbuf = [&](int b) { return smem + C::D_OFF + b * C::CAND_SLOT; };
 
-    // Thread 0: prefetch of step t's entering (and leaving) planes.
+    // Thread 0: loads of step t's planes into A buffer t&1 (slot 0: the entering
+    // plane, slot 1: the second warm-up plane or the leaving plane).
     auto issueA = [&](int t) {
         const int b = t & 1, pass = t / SPP, s = t - pass * SPP;
         const int oz = pass / C::K - M, oy = pass % C::K - M;
-        const int ep = Z0 + M + s;  // padded plane of the entering plane (unpadded Z0 - N + s)
-        const bool leave = s >= 2 * N + 1;
+        int p0, p1 = -1;
+        if (s < N) {
+            p0 = Z0 + M + 2 * s;
+            p1 = p0 + 1;
+        } else {
+            const int q = s - N;
+            p0 = Z0 + M + 2 * N + q;
+            if (q >= 1) p1 = Z0 + M + q - 1;
+        }
         unsigned char* base = abuf(b);
+        const int xr = X0 - 4 + 4 * C::G0, yr = Y0 + M;
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&barA[b], (leave ? 2u : 1u) * (C::REF_TX + C::CAND_TX));
-        tma_load_3d(base, &mapR, X0 - 4 + 4 * C::G0, Y0 + M, ep, &barA[b]);
-        tma_load_3d(base + 2 * C::REF_SLOT, &mapC, X0 - 4, Y0 + M + oy, ep + oz, &barA[b]);
-        if (leave) {
-            const int lp = ep - (2 * N + 1);
-            tma_load_3d(base + C::REF_SLOT, &mapR, X0 - 4 + 4 * C::G0, Y0 + M, lp, &barA[b]);
-            tma_load_3d(base + 2 * C::REF_SLOT + C::CAND_SLOT, &mapC, X0 - 4, Y0 + M + oy, lp + oz,
+        mbar_arrive_expect_tx(&barA[b], (p1 >= 0 ? 2u : 1u) * (C::REF_TX + C::CAND_TX));
+        tma_load_3d(base, &mapR, xr, yr, p0, &barA[b]);
+        tma_load_3d(base + 2 * C::REF_SLOT, &mapC, X0 - 4, yr + oy, p0 + oz, &barA[b]);
+        if (p1 >= 0) {
+            tma_load_3d(base + C::REF_SLOT, &mapR, xr, yr, p1, &barA[b]);
+            tma_load_3d(base + 2 * C::REF_SLOT + C::CAND_SLOT, &mapC, X0 - 4, yr + oy, p1 + oz,
                         &barA[b]);
         }
     };
@@ -151,9 +165,10 @@ __global__ void __launch_bounds__(512, 1)
         issueD(0);
     }
 
-    // Stage A ownership: group gi (columns 4*(G0+gi) .. +3 of the box), halo row ya.
-    const int gi = tid % C::NG, ya = tid / C::NG;
-    const bool hasA = tid < C::NA;
+    // Stage A ownership: 16 lanes per halo row (conflict-free shared loads), lane
+    // gi < NG owns columns 4*(G0+gi) .. +3 of the box.
+    const int gi = tid & 15, ya = tid >> 4;
+    const bool hasA = gi < C::NG && ya < C::HY;
     float Sz[C::K][4];
 
     int d = 0;  // output steps done
@@ -166,49 +181,70 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) Sz[k][c] = 0.f;
         }
+        const bool out_step = s >= N;
+        // Stage D's partial sums of this voxel from earlier passes, requested now so
+        // the load overlaps stages A-C.
+        const int vy = tid >> 5, vj = tid & 31;
+        const int vx = X0 + vj, vyy = Y0 + vy, vz = Z0 + (s - N);
+        const bool vin = out_step && vx < a.X && vyy < a.Y;
+        const size_t vo = ((size_t)vz * a.Y + vyy) * a.X + vx;
+        float2 prev = make_float2(0.f, 0.f);
+        if (vin && pass > 0) prev = a.acc[vo];
         const int b = t & 1;
         const bool okA = mbar_wait_bounded(&barA[b], (t >> 1) & 1);
         if (!okA) {
             raise_device_error(a.errword, DEVERR_TMA_TIMEOUT);
             s_abort = 1;
         }
-        const bool out_step = s >= 2 * N;
         if (okA && hasA) {
-            const float* refE = reinterpret_cast<const float*>(abuf(b));
-            const float* refL = refE + C::REF_SLOT / 4;
-            const float* candE = refE + 2 * C::REF_SLOT / 4;
-            const float* candL = candE + C::CAND_SLOT / 4;
-            const float4 ae = *reinterpret_cast<const float4*>(refE + ya * C::BWR + 4 * gi);
-            float ce[4 * (2 * C::R + 1)];
+            const float* ref0 = reinterpret_cast<const float*>(abuf(b));
+            const float* ref1 = ref0 + C::REF_SLOT / 4;
+            const float* cand0 = ref0 + 2 * C::REF_SLOT / 4;
+            const float* cand1 = cand0 + C::CAND_SLOT / 4;
             const int g = C::G0 + gi;
+            const float4 a0 = *reinterpret_cast<const float4*>(ref0 + ya * C::BWR + 4 * gi);
+            const float av[4] = {a0.x, a0.y, a0.z, a0.w};
+            float c0[4 * (2 * C::R + 1)];
 #pragma unroll
             for (int r = 0; r <= 2 * C::R; ++r)
-                *reinterpret_cast<float4*>(&ce[4 * r]) =
-                    *reinterpret_cast<const float4*>(candE + ya * C::BWC + 4 * (g - C::R + r));
-            const float av[4] = {ae.x, ae.y, ae.z, ae.w};
-            if (s >= 2 * N + 1) {
-                const float4 al = *reinterpret_cast<const float4*>(refL + ya * C::BWR + 4 * gi);
-                float cl[4 * (2 * C::R + 1)];
+                *reinterpret_cast<float4*>(&c0[4 * r]) =
+                    *reinterpret_cast<const float4*>(cand0 + ya * C::BWC + 4 * (g - C::R + r));
+            if (s != N) {
+                // second plane: added (warm-up) or dropped (leaving)
+                const float4 a1 = *reinterpret_cast<const float4*>(ref1 + ya * C::BWR + 4 * gi);
+                const float lv[4] = {a1.x, a1.y, a1.z, a1.w};
+                float c1[4 * (2 * C::R + 1)];
 #pragma unroll
                 for (int r = 0; r <= 2 * C::R; ++r)
-                    *reinterpret_cast<float4*>(&cl[4 * r]) =
-                        *reinterpret_cast<const float4*>(candL + ya * C::BWC + 4 * (g - C::R + r));
-                const float lv[4] = {al.x, al.y, al.z, al.w};
+                    *reinterpret_cast<float4*>(&c1[4 * r]) =
+                        *reinterpret_cast<const float4*>(cand1 + ya * C::BWC + 4 * (g - C::R + r));
+                if (s < N) {
 #pragma unroll
-                for (int k = 0; k < C::K; ++k)
+                    for (int k = 0; k < C::K; ++k)
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const int i = 4 * C::R + c + k - M;
-                        const float de = av[c] - ce[i];
-                        const float dl = lv[c] - cl[i];
-                        Sz[k][c] = fmaf(-dl, dl, fmaf(de, de, Sz[k][c]));
-                    }
+                        for (int c = 0; c < 4; ++c) {
+                            const int i = 4 * C::R + c + k - M;
+                            const float de = av[c] - c0[i];
+                            const float dl = lv[c] - c1[i];
+                            Sz[k][c] = fmaf(dl, dl, fmaf(de, de, Sz[k][c]));
+                        }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < C::K; ++k)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const int i = 4 * C::R + c + k - M;
+                            const float de = av[c] - c0[i];
+                            const float dl = lv[c] - c1[i];
+                            Sz[k][c] = fmaf(-dl, dl, fmaf(de, de, Sz[k][c]));
+                        }
+                }
             } else {
 #pragma unroll
                 for (int k = 0; k < C::K; ++k)
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        const float de = av[c] - ce[4 * C::R + c + k - M];
+                        const float de = av[c] - c0[4 * C::R + c + k - M];
                         Sz[k][c] = fmaf(de, de, Sz[k][c]);
                     }
             }
@@ -224,7 +260,7 @@ __global__ void __launch_bounds__(512, 1)
         if (!out_step) continue;
         if (tid == 0 && d + 1 < TD) issueD(lastD = d + 1);
 
-        // B: x box sums along halo rows.
+        // B: x box sums along halo rows, two independent running sums of 16 outputs.
         if (tid < C::NB) {
             const int k = tid / C::HY, yh = tid - k * C::HY;
             const float* row = Szb + (k * C::HY + yh) * C::PSZ;
@@ -233,37 +269,54 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
             for (int q = 0; q < NV; ++q)
                 *reinterpret_cast<float4*>(&v[4 * q]) = *reinterpret_cast<const float4*>(row + 4 * q);
-            float* sx = Sxb + (k * C::HY + yh) * C::PSX;
-            float acc = 0.f;
+            float o[C::CX];
+            float acc[2];
 #pragma unroll
-            for (int x = 0; x <= 2 * N; ++x) acc += v[C::MA + x];
-            float o[4];
-            o[0] = acc;
+            for (int sg = 0; sg < 2; ++sg) {
+                acc[sg] = 0.f;
 #pragma unroll
-            for (int j = 1; j < C::CX; ++j) {
-                acc += v[C::MA + j + 2 * N] - v[C::MA + j - 1];
-                o[j & 3] = acc;
-                if ((j & 3) == 3)
-                    *reinterpret_cast<float4*>(sx + j - 3) = make_float4(o[0], o[1], o[2], o[3]);
+                for (int x = 0; x <= 2 * N; ++x) acc[sg] += v[C::MA + 16 * sg + x];
+                o[16 * sg] = acc[sg];
             }
+#pragma unroll
+            for (int j = 1; j < 16; ++j)
+#pragma unroll
+                for (int sg = 0; sg < 2; ++sg) {
+                    const int jj = 16 * sg + j;
+                    acc[sg] += v[C::MA + jj + 2 * N] - v[C::MA + jj - 1];
+                    o[jj] = acc[sg];
+                }
+            float* sx = Sxb + (k * C::HY + yh) * C::PSX;
+#pragma unroll
+            for (int q = 0; q < C::CX / 4; ++q)
+                *reinterpret_cast<float4*>(sx + 4 * q) =
+                    make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
         }
         __syncthreads();
-        // C: y box sums down output columns, in place (row y of the column becomes D).
+        // C: y box sums down output columns, in place (row y of the column becomes D),
+        // two independent running sums of 8 outputs.
         if (tid < C::NC) {
             const int k = tid >> 5, j = tid & 31;
             float* col = Sxb + k * C::HY * C::PSX + j;
             float u[C::HY];
 #pragma unroll
             for (int yh = 0; yh < C::HY; ++yh) u[yh] = col[yh * C::PSX];
-            float acc = 0.f;
+            float acc[2];
 #pragma unroll
-            for (int y = 0; y <= 2 * N; ++y) acc += u[y];
-            col[0] = acc;
+            for (int sg = 0; sg < 2; ++sg) {
+                acc[sg] = 0.f;
 #pragma unroll
-            for (int y = 1; y < C::CY; ++y) {
-                acc += u[y + 2 * N] - u[y - 1];
-                col[y * C::PSX] = acc;
+                for (int y = 0; y <= 2 * N; ++y) acc[sg] += u[8 * sg + y];
+                col[8 * sg * C::PSX] = acc[sg];
             }
+#pragma unroll
+            for (int y = 1; y < 8; ++y)
+#pragma unroll
+                for (int sg = 0; sg < 2; ++sg) {
+                    const int yy = 8 * sg + y;
+                    acc[sg] += u[yy + 2 * N] - u[yy - 1];
+                    col[yy * C::PSX] = acc[sg];
+                }
         }
         __syncthreads();
         // D: weights and accumulation for voxel (X0 + j, Y0 + y, z).
@@ -274,29 +327,24 @@ __global__ void __launch_bounds__(512, 1)
                 raise_device_error(a.errword, DEVERR_TMA_TIMEOUT);
                 s_abort = 1;
             } else {
-                const int y = tid >> 5, j = tid & 31;
-                const int dpass = d / TZc, q = d - dpass * TZc;
-                const int x = X0 + j, yy = Y0 + y, z = Z0 + q;
-                const bool inside = x < a.X && yy < a.Y;
-                const size_t o = ((size_t)z * a.Y + yy) * a.X + x;
-                float2 prev = make_float2(0.f, 0.f);
-                if (inside && dpass > 0) prev = a.acc[o];
-                const float* cpl = reinterpret_cast<const float*>(dbuf(db)) + (N + y) * C::BWC + 4 + N + j;
-                float zl = 0.f, nl = 0.f;
+                const int y = vy, j = vj;
+                const float* cpl =
+                    reinterpret_cast<const float*>(dbuf(db)) + (N + y) * C::BWC + 4 + N + j;
+                float zl[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < C::K; ++k) {
                     const float w = ex2_neg(Sxb[(k * C::HY + y) * C::PSX + j]);
-                    zl += w;
-                    nl = fmaf(w, cpl[k], nl);
+                    zl[k & 1] += w;
+                    nl[k & 1] = fmaf(w, cpl[k], nl[k & 1]);
                 }
-                if (inside) {
-                    zl = prev.x + zl;
-                    nl = prev.y + nl;
-                    if (dpass == P - 1) {
-                        a.out[o] = nl / zl * a.inv_scale;
-                        if (a.zsum) a.zsum[o] = zl;
+                if (vin) {
+                    const float zt = prev.x + (zl[0] + zl[1]);
+                    const float nt = prev.y + (nl[0] + nl[1]);
+                    if (pass == P - 1) {
+                        a.out[vo] = nt / zt * a.inv_scale;
+                        if (a.zsum) a.zsum[vo] = zt;
                     } else {
-                        a.acc[o] = make_float2(zl, nl);
+                        a.acc[vo] = make_float2(zt, nt);
                     }
                 }
             }

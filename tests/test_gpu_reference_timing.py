@@ -121,3 +121,72 @@ def test_reference_2d_kernels_vs_repo_kernel_2048(torch_cuda, gnlm_lib):
           f"; this repo {t_mine:.3f} ms ({X * X / t_mine / 1e3:.1f} Mpixel/s), "
           f"speed-up vs fastest reference variant {best / t_mine:.2f}x")
     assert t_mine < best
+
+
+def _ref3d_variants(SS, NS, X):
+    """(name, grid.x, mangled symbol) of the four kernels the reference's launcher
+    runs (3DNLM/main.cu:7626-7666): the generic kernel and shift_1..3."""
+    gen = ("generic", (X + 32 - NS) // (33 - NS), R.K3D)
+    shifts = [(f"shift_{s}", (X + 31 - s) // (32 - s), R._mangle(f"NLmeansOnGPU_shift_{s}", "PhPfS0_"))
+              for s in (1, 2, 3)]
+    return [gen] + shifts
+
+
+def _ref3d_slack_top(SS, NS, X, Y, depth):
+    """Upper bound of the element index any of the four kernels reads.  Their row
+    and plane indices stay inside the padded volume at these sizes; the x index of
+    a lane runs at most (SS - 1) + (NS - 1) past its lane column ix (3DNLM/main.cu
+    :59,111 and the shift kernels' `k + ix + c` terms with c <= NS - 1, e.g.
+    :6254-7599 for NS = 17), and ix <= (grid.x - 1) * step + 31."""
+    W, H, Dp = X + SS + NS - 2, Y + SS + NS - 2, depth + SS + NS - 2
+    steps = {"generic": 33 - NS, "shift_1": 31, "shift_2": 30, "shift_3": 29}
+    ix_max = max((g - 1) * steps[name] + 31 for name, g, _ in _ref3d_variants(SS, NS, X))
+    return (Dp * H - 1) * W + ix_max + SS + NS
+
+
+@pytest.mark.parametrize("SS,NS", [(11, 13), (11, 15), (11, 17), (13, 13), (13, 15), (13, 17)])
+def test_reference_large_patch_kernels_vs_repo_kernel(torch_cuda, gnlm_lib, SS, NS):
+    """The reference's sweep sizes (3DNLM/run.sh:25-34) at depth 16: its four kernels
+    against this repo's large-patch kernel on the same pre-padded uchar volume."""
+    torch = torch_cuda
+    X = Y = 512
+    D = 16
+    cubin = os.path.join(R.REF_DIR, f"ref3d_ss{SS}_ns{NS}_x{X}_y{Y}_d{D}.cubin")
+    if not os.path.exists(cubin):
+        pytest.skip("reference cubins not built here")
+    W, H, Dp = X + SS + NS - 2, Y + SS + NS - 2, D + SS + NS - 2
+    size = W * H * Dp
+    top = _ref3d_slack_top(SS, NS, X, Y, D)
+    from gnlm import phantom
+    import oracle as O
+    img = np.clip(phantom.disc_rect_phantom((Y, X), n_shapes=32, sigma=0.03, seed=NS)[0] * 255,
+                  0, 255).astype(np.uint8)
+    p2 = O.pad_reflect101(img, (SS + NS - 2) // 2)
+    padded = np.ascontiguousarray(np.broadcast_to(p2, (Dp, H, W)))
+    buf = torch.zeros(max(size, top + 1) + 4096, dtype=torch.uint8, device="cuda")
+    buf[:size].copy_(torch.from_numpy(padded.ravel()))
+    out = torch.zeros(D * Y * X, dtype=torch.float32, device="cuda")
+    variants = _ref3d_variants(SS, NS, X)
+    n_w = max(g for _, g, _ in variants) * 32 * 64 * 4 * SS ** 3  # 3DNLM/main.cu:7618
+    weight = torch.zeros(n_w, dtype=torch.float32, device="cuda")
+    drv = R.Driver()
+    P = ctypes.c_void_p
+    args = [P(buf.data_ptr()), P(out.data_ptr()), P(weight.data_ptr())]
+    times = {}
+    for name, g, sym in variants:
+        fn = drv.function(cubin, sym)
+        times[name] = _time(torch, lambda: drv.launch(fn, (g, 16, 4), (32, 4, 1), args), reps=1)
+    x = buf[:size].reshape(Dp, H, W)
+    mine_out = torch.empty((D, Y, X), dtype=torch.float32, device="cuda")
+    sr, pr = (SS - 1) // 2, (NS - 1) // 2
+
+    def mine():
+        gnlm_lib.nlm3d_forward(x, sr, pr, 10.0, prepadded=True, shape=(D, Y, X), out=mine_out)
+
+    t_mine = _time(torch, mine)
+    best = min(times.values())
+    print(f"\n3D 512x512x{D} SS{SS} NS{NS}: reference " +
+          ", ".join(f"{k} {v:.1f} ms" for k, v in times.items()) +
+          f"; this repo {t_mine:.2f} ms ({X * Y * D / t_mine / 1e3:.1f} Mvoxel/s), "
+          f"speed-up vs fastest reference kernel {best / t_mine:.1f}x")
+    assert t_mine < best
