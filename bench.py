@@ -233,6 +233,38 @@ def bench_2d(torch, gnlm, reps=5):
             "autotune_ms": [round(v, 4) for v in tune]}
 
 
+def bench_large_patch(torch, gnlm, reps=3):
+    """The largest configuration of the reference's large-patch sweep: 512 x 512 x 128,
+    search 13^3 (sr 6), patch 17^3 (pr 8), h 0.05, 48 ellipsoids sigma 0.05; staging +
+    large-patch kernel per call."""
+    from gnlm import phantom
+    shape, sr, pr = (128, 512, 512), 6, 8
+    v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=48, sigma=0.05, seed=4)
+    x = torch.from_numpy(v).cuda()
+    best, tune = gnlm.autotune(3, shape, sr, pr)
+    out = torch.empty_like(x)
+    gnlm.nlm3d_forward(x, sr, pr, 0.05, out=out)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        gnlm.nlm3d_forward(x, sr, pr, 0.05, out=out)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = min(ms)
+    nvox = shape[0] * shape[1] * shape[2]
+    pairs = nvox * (2 * sr + 1) ** 3
+    gnlm.set_variant(3, sr, pr, -1)
+    return {"shape": list(shape), "search_radius": sr, "patch_radius": pr, "ms": round(t, 3),
+            "value": round(nvox / (t * 1e-3) / 1e6, 2), "unit": "Mvoxel/s",
+            "gpairs_per_s": round(pairs / (t * 1e-3) / 1e9, 1),
+            "tflops": round(FLOPS_PER_PAIR * pairs / (t * 1e-3) / 1e12, 2),
+            "kernel": "nlm3d_lp_kernel<6,8>", "variant": best,
+            "autotune_ms": [round(v, 3) for v in tune]}
+
+
 def bench_adjoint(torch, gnlm, steps=50):
     """128^3 (ellipsoids, sigma 0.05, sr 3, pr 1): forward + adjoint per step, used
     to fit h by gradient descent on the MSE to the clean phantom."""
@@ -429,6 +461,7 @@ def run_gnlm(args):
     batched = bench_batched(torch, gnlm) if not args.skip_extra else None
     adjoint = bench_adjoint(torch, gnlm) if not args.skip_extra else None
     image2d = bench_2d(torch, gnlm) if not args.skip_extra else None
+    large = bench_large_patch(torch, gnlm) if not args.skip_extra else None
     fused_mean = statistics.mean(fused_ms)
     achieved = FLOPS_PER_PAIR * OFFSETS * nvox / (fused_mean * 1e-3) / 1e12
     traffic = read_profile_traffic("nlm3d_fwd_kernel")
@@ -462,6 +495,7 @@ def run_gnlm(args):
                   "batched": batched},
         "adjoint": adjoint,
         "nlm2d": image2d,
+        "large_patch": large,
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:
