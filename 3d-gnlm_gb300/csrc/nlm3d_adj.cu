@@ -125,15 +125,19 @@ __global__ void __launch_bounds__(32 * NW, 1)
     const int sx = lane + C::HE + ral;
     const int sy = warp * RY + C::HE;
     const int sz = C::HE;
-    // v' values of the difference window (same for every offset)
-    float av[C::RT][C::PT];
+    // v' values of the difference window (same for every offset), as row pairs
+    static_assert(C::RT % 2 == 0, "row pairs");
+    constexpr int RTP = C::RT / 2;
+    float2 av[RTP][C::PT];
     // G and out' at the distance window (same for every offset)
     float gu[C::RD][C::PD], ou[C::RD][C::PD];
 #pragma unroll
-    for (int r = 0; r < C::RT; ++r)
+    for (int rp = 0; rp < RTP; ++rp)
 #pragma unroll
-        for (int p = 0; p < C::PT; ++p)
-            av[r][p] = vt[(sz + p - 2 * N) * C::PLANE + (sy + r - 2 * N) * C::BX + sx];
+        for (int p = 0; p < C::PT; ++p) {
+            const int i = (sz + p - 2 * N) * C::PLANE + (sy + 2 * rp - 2 * N) * C::BX + sx;
+            av[rp][p] = make_float2(vt[i], vt[i + C::BX]);
+        }
 #pragma unroll
     for (int r = 0; r < C::RD; ++r)
 #pragma unroll
@@ -142,6 +146,7 @@ __global__ void __launch_bounds__(32 * NW, 1)
             gu[r][p] = gt[i];
             ou[r][p] = ot[i];
         }
+    auto avs = [&](int r, int p) { return (r & 1) ? av[r >> 1][p].y : av[r >> 1][p].x; };
 
     float acc[RY][RZ];
 #pragma unroll
@@ -149,35 +154,56 @@ __global__ void __launch_bounds__(32 * NW, 1)
 #pragma unroll
         for (int q = 0; q < RZ; ++q) acc[r][q] = 0.f;
     double hacc = 0.0;
+    const float2 minus1 = make_float2(-1.f, -1.f);
 
     for (int oz = -M; oz <= M; ++oz) {
         for (int oy = -M; oy <= M; ++oy) {
+            // dL/dh terms of this run of 2M+1 offsets, summed in FP32, then added to
+            // the FP64 total once per run
+            float hrun = 0.f;
             for (int ox = -M; ox <= M; ++ox) {
                 const int off = oz * C::PLANE + oy * C::BX + ox;
-                // differences t over the window, candidate values b
-                float t[C::RT][C::PT], bv[C::RD][C::PD];
+                // differences t = v'_u - v'_{u+o} over the window (row pairs), candidates b
+                float2 t2[RTP][C::PT];
+                float bv[C::RD][C::PD];
 #pragma unroll
-                for (int r = 0; r < C::RT; ++r)
+                for (int rp = 0; rp < RTP; ++rp)
 #pragma unroll
                     for (int p = 0; p < C::PT; ++p) {
-                        const float b =
-                            vt[(sz + p - 2 * N) * C::PLANE + (sy + r - 2 * N) * C::BX + sx + off];
-                        t[r][p] = av[r][p] - b;
-                        if (r >= N && r < N + C::RD && p >= N && p < N + C::PD)
-                            bv[r - N][p - N] = b;
+                        const int i =
+                            (sz + p - 2 * N) * C::PLANE + (sy + 2 * rp - 2 * N) * C::BX + sx + off;
+                        const float b0 = vt[i], b1 = vt[i + C::BX];
+                        t2[rp][p] = __ffma2_rn(make_float2(b0, b1), minus1, av[rp][p]);
+                        const int r0 = 2 * rp, r1 = 2 * rp + 1;
+                        if (p >= N && p < N + C::PD) {
+                            if (r0 >= N && r0 < N + C::RD) bv[r0 - N][p - N] = b0;
+                            if (r1 >= N && r1 < N + C::RD) bv[r1 - N][p - N] = b1;
+                        }
                     }
-                // distance D' on the distance window: z, y, then x across lanes
+                auto ts = [&](int r, int p) { return (r & 1) ? t2[r >> 1][p].y : t2[r >> 1][p].x; };
+                // distance D' on the distance window: z sums of t^2 (packed row pairs),
+                // then y sums, then x across lanes
+                float2 zs[RTP][C::PD];
+#pragma unroll
+                for (int rp = 0; rp < RTP; ++rp)
+#pragma unroll
+                    for (int p = 0; p < C::PD; ++p) {
+                        float2 sum = __fmul2_rn(t2[rp][p], t2[rp][p]);
+#pragma unroll
+                        for (int kz = 1; kz < C::K; ++kz)
+                            sum = __ffma2_rn(t2[rp][p + kz], t2[rp][p + kz], sum);
+                        zs[rp][p] = sum;
+                    }
+                auto zss = [&](int r, int p) { return (r & 1) ? zs[r >> 1][p].y : zs[r >> 1][p].x; };
                 float D[C::RD][C::PD];
 #pragma unroll
                 for (int r = 0; r < C::RD; ++r)
 #pragma unroll
                     for (int p = 0; p < C::PD; ++p) {
-                        float s = 0.f;
+                        float sum = zss(r, p);
 #pragma unroll
-                        for (int ky = 0; ky < C::K; ++ky)
-#pragma unroll
-                            for (int kz = 0; kz < C::K; ++kz) s = fmaf(t[r + ky][p + kz], t[r + ky][p + kz], s);
-                        D[r][p] = s;
+                        for (int ky = 1; ky < C::K; ++ky) sum += zss(r + ky, p);
+                        D[r][p] = sum;
                     }
 #pragma unroll
                 for (int r = 0; r < C::RD; ++r)
@@ -190,7 +216,7 @@ __global__ void __launch_bounds__(32 * NW, 1)
                             xv += __shfl_down_sync(0xffffffffu, yv, k) + __shfl_up_sync(0xffffffffu, yv, k);
                         D[r][p] = xv;
                     }
-                // weights, G(u+o), out'(u+o), and the field a_o(u) (without the -ln2)
+                // weights, G(u+o), and the field a_o(u) (without the -ln2)
                 float e[C::RD][C::PD], a[C::RD][C::PD], guo[C::RD][C::PD];
 #pragma unroll
                 for (int r = 0; r < C::RD; ++r)
@@ -200,41 +226,41 @@ __global__ void __launch_bounds__(32 * NW, 1)
                         const float g2 = gt[i], o2 = ot[i];
                         e[r][p] = ex2_neg(D[r][p]);
                         guo[r][p] = g2;
-                        const float vu = av[r + N][p + N];
+                        const float vu = avs(r + N, p + N);
                         a[r][p] = e[r][p] * fmaf(gu[r][p], bv[r][p] - ou[r][p], g2 * (vu - o2));
                     }
-                // h partial: a1 at the thread's own voxels (lanes/rows/planes checked below)
-                // box sum of a over the patch: z, y, then x across lanes
-                float A[RY][RZ];
+                // box sum of a over the patch: z, then y, then x across lanes
+                float za[C::RD][RZ];
 #pragma unroll
-                for (int r = 0; r < RY; ++r)
+                for (int r = 0; r < C::RD; ++r)
 #pragma unroll
                     for (int q = 0; q < RZ; ++q) {
-                        float s = 0.f;
+                        float sum = a[r][q];
 #pragma unroll
-                        for (int ky = 0; ky < C::K; ++ky)
-#pragma unroll
-                            for (int kz = 0; kz < C::K; ++kz) s += a[r + ky][q + kz];
-                        A[r][q] = s;
+                        for (int kz = 1; kz < C::K; ++kz) sum += a[r][q + kz];
+                        za[r][q] = sum;
                     }
 #pragma unroll
                 for (int r = 0; r < RY; ++r)
 #pragma unroll
                     for (int q = 0; q < RZ; ++q) {
-                        const float yv = A[r][q];
+                        float yv = za[r][q];
+#pragma unroll
+                        for (int ky = 1; ky < C::K; ++ky) yv += za[r + ky][q];
                         float xv = yv;
 #pragma unroll
                         for (int k = 1; k <= N; ++k)
                             xv += __shfl_down_sync(0xffffffffu, yv, k) + __shfl_up_sync(0xffffffffu, yv, k);
                         // gpad' += G(q+o) e_q(o) + 2 (v'_q - v'_{q+o}) (-ln2) A(q)
                         acc[r][q] = fmaf(guo[r + N][q + N], e[r + N][q + N], acc[r][q]);
-                        acc[r][q] = fmaf(-2.f * kLn2 * t[r + 2 * N][q + 2 * N], xv, acc[r][q]);
+                        acc[r][q] = fmaf(-2.f * kLn2 * ts(r + 2 * N, q + 2 * N), xv, acc[r][q]);
                         // dL/dh partial: a1_o(q) D'_q(o), a1 = -ln2 e G(q) (v'_{q+o} - out'_q)
                         const float a1 = e[r + N][q + N] * gu[r + N][q + N] *
                                          (bv[r + N][q + N] - ou[r + N][q + N]);
-                        hacc += (double)(a1 * D[r + N][q + N]);
+                        hrun = fmaf(a1, D[r + N][q + N], hrun);
                     }
             }
+            hacc += (double)hrun;
         }
     }
 
