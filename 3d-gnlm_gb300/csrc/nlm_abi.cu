@@ -44,9 +44,10 @@ std::map<int, unsigned int*> g_errword;                    // device -> error wo
 std::map<std::pair<int, cudaStream_t>, std::pair<void*, size_t>> g_ws;  // cached workspaces
 
 struct HostPath {
-    cudaStream_t stream = nullptr;  // staging + compute
+    cudaStream_t stream = nullptr;  // staging + compute (even chunks of the pipelined path)
+    cudaStream_t s_c2 = nullptr;    // staging + compute of odd chunks
     cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
-    std::vector<cudaEvent_t> ev_in, ev_out;
+    std::vector<cudaEvent_t> ev_in, ev_out, ev_st;
     void* d_in = nullptr;
     size_t in_bytes = 0;
     float* d_out = nullptr;
@@ -243,7 +244,8 @@ int nlm_release_cached(void) {
         HostPath* hp = kv.second;
         cudaSetDevice(kv.first);
         std::lock_guard<std::mutex> hl(hp->mu);
-        if (hp->stream) cudaStreamSynchronize(hp->stream);
+        for (cudaStream_t st : {hp->stream, hp->s_c2, hp->s_h2d, hp->s_d2h})
+            if (st) cudaStreamSynchronize(st);
         cudaFree(hp->d_in);
         cudaFree(hp->d_out);
         cudaFree(hp->d_ws);
@@ -497,7 +499,11 @@ static int ensure_events(std::vector<cudaEvent_t>& v, size_t n) {
 // chunks and the device->host copy of finished output chunks overlap the staging
 // and NLM kernels of the current chunk.  Output chunk k = planes [k CZ, (k+1) CZ),
 // CZ a multiple of the kernel's z tile; it waits only for the input planes its
-// REFLECT_101 halo reaches.  Returns 1 when the volume is too thin to split.
+// REFLECT_101 halo reaches.  Chunks alternate between two compute streams so that
+// the kernels of chunk k+1 fill the SMs that chunk k's last wave leaves idle: chunk
+// k stages padded planes [z0 + 2H, z1 + 2H) (all of [0, z1 + 2H) for k = 0), which no
+// earlier chunk reads, and its NLM kernel waits for the staging of chunk k-1, which
+// wrote the lower 2H planes it reads.  Returns 1 when the volume is too thin to split.
 static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype, int X, int Y,
                                     int Z, int sr, int pr, float h, float* h_out,
                                     unsigned int flags) {
@@ -513,6 +519,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     cudaError_t e = cudaSuccess;
     if (!hp->s_h2d) e = cudaStreamCreateWithFlags(&hp->s_h2d, cudaStreamNonBlocking);
     if (e == cudaSuccess && !hp->s_d2h) e = cudaStreamCreateWithFlags(&hp->s_d2h, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !hp->s_c2) e = cudaStreamCreateWithFlags(&hp->s_c2, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
     const Staging st = staging3d(X, Y, Z, H, fp16);
     const size_t plane_in =
@@ -521,6 +528,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const int nin = (in_planes + CZ - 1) / CZ;
     int rc = ensure_events(hp->ev_in, nin);
     if (rc == NLM_OK) rc = ensure_events(hp->ev_out, nch);
+    if (rc == NLM_OK) rc = ensure_events(hp->ev_st, nch);
     if (rc != NLM_OK) return rc;
     const char* src = static_cast<const char*>(h_in);
     char* din = static_cast<char*>(hp->d_in);
@@ -539,12 +547,15 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
         const int p0 = k == 0 ? 0 : z0 + 2 * H, p1 = z1 + 2 * H;  // new padded planes
         const int need = prepadded ? p1 - 1 : std::min(Z, z1 + H) - 1;  // last input plane read
         const int j = std::min(nin - 1, need / CZ);
-        e = cudaStreamWaitEvent(hp->stream, hp->ev_in[j], 0);
-        if (e == cudaSuccess) e = launch_stage(hp->d_in, in_dtype, prepadded, s, st, hp->d_ws, hp->stream, p0, p1);
+        cudaStream_t cs = (k & 1) ? hp->s_c2 : hp->stream;
+        e = cudaStreamWaitEvent(cs, hp->ev_in[j], 0);
+        if (e == cudaSuccess) e = launch_stage(hp->d_in, in_dtype, prepadded, s, st, hp->d_ws, cs, p0, p1);
+        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_st[k], cs);
+        if (e == cudaSuccess && k > 0) e = cudaStreamWaitEvent(cs, hp->ev_st[k - 1], 0);
         if (e == cudaSuccess)
             e = launch_nlm3d_fwd(st, hp->d_ws, sr, pr, fp16, variant, 1.0f / s, hp->d_out, nullptr,
-                                 ew, hp->stream, z0 / RZ, (z1 + RZ - 1) / RZ);
-        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_out[k], hp->stream);
+                                 ew, cs, z0 / RZ, (z1 + RZ - 1) / RZ);
+        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_out[k], cs);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(hp->s_d2h, hp->ev_out[k], 0);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(h_out + (size_t)z0 * plane_out, hp->d_out + (size_t)z0 * plane_out,
@@ -554,6 +565,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     }
     e = cudaStreamSynchronize(hp->s_d2h);
     if (e == cudaSuccess) e = cudaStreamSynchronize(hp->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(hp->s_c2);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
     return NLM_OK;
 }
