@@ -26,6 +26,25 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                                                   errword);
 }
 
+// Single-volume kernel with paired z offsets (fwd3d_tile_pz).
+template <int M, int N, int RY, int RZ, int NW, int MINB>
+__global__ void __launch_bounds__(32 * NW, MINB)
+    nlm3d_fwd_pz_kernel(const __grid_constant__ CUtensorMap tmap, int X, int Y, int Z,
+                        float inv_scale, float* __restrict__ out, float* __restrict__ zsum,
+                        unsigned int* errword, int bz0) {
+    using C = Fwd3d<M, N, float, RY, RZ, NW>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* tile = reinterpret_cast<float*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    fwd3d_tile_pz<M, N, RY, RZ, NW>(&tmap, tile, bar, 0, blockIdx.x, blockIdx.y, blockIdx.z + bz0,
+                                    X, Y, Z, inv_scale, out, zsum, errword);
+}
+
 // FP16-storage single-volume kernel (row-pair layout, two tensor maps).
 template <int M, int N, int RY, int RZ, int NW, int MINB, bool KAHAN>
 __global__ void __launch_bounds__(32 * NW, MINB)
@@ -71,6 +90,28 @@ static cudaError_t run_fwd3d_h2(const Staging& st, const void* staged, float inv
     return cudaGetLastError();
 }
 
+template <int M, int N, int RY, int RZ, int NW, int MINB>
+static cudaError_t run_fwd3d_pz(const Staging& st, const void* staged, float inv_scale, float* out,
+                                float* zsum, unsigned int* errword, cudaStream_t stream, int zt0,
+                                int zt1) {
+    using C = Fwd3d<M, N, float, RY, RZ, NW>;
+    CUtensorMap map;
+    const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
+    const uint64_t strides[2] = {(uint64_t)st.Xs * 4, (uint64_t)st.Xs * st.Yp * 4};
+    const uint32_t box[3] = {(uint32_t)C::BX, (uint32_t)C::BY, (uint32_t)C::BZ};
+    cudaError_t e = encode_tensor_map(&map, false, 3, dims, strides, box, const_cast<void*>(staged));
+    if (e != cudaSuccess) return e;
+    auto kern = nlm3d_fwd_pz_kernel<M, N, RY, RZ, NW, MINB>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    if (zt1 < 0) zt1 = (st.Z + RZ - 1) / RZ;
+    if (zt1 <= zt0) return cudaSuccess;
+    dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY, zt1 - zt0);
+    kern<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(map, st.X, st.Y, st.Z, inv_scale, out, zsum,
+                                                      errword, zt0);
+    return cudaGetLastError();
+}
+
 template <int M, int N, typename T, int RY, int RZ, int NW, int MINB, bool AREG, bool KAHAN>
 static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_scale, float* out,
                              float* zsum, unsigned int* errword, cudaStream_t stream, int zt0,
@@ -103,6 +144,8 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
 //   1: 4 x 8, reference values re-read from shared memory, 3 CTAs/SM
 //   2: 4 x 4, registers, 3 CTAs/SM
 //   3: 2 x 8, registers, 3 CTAs/SM
+//   4: 4 x 8, registers, z offsets in pairs sharing candidate planes, 2 CTAs/SM
+//   5: 4 x 6, as 4
 // FP16-storage form (row-pair layout, Kahan-compensated weight sum):
 //   0: 4 x 6, 2 CTAs/SM;  1: 4 x 8, 2 CTAs/SM;  2: 2 x 8, 3 CTAs/SM
 template <int m, int n>
@@ -115,6 +158,8 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
             case 1: return run_fwd3d<m, n, float, 4, 8, 4, 3, false, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 2: return run_fwd3d<m, n, float, 4, 4, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 3: return run_fwd3d<m, n, float, 2, 8, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 4: return run_fwd3d_pz<m, n, 4, 8, 4, 2>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 5: return run_fwd3d_pz<m, n, 4, 6, 4, 2>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
         }
     } else {
         switch (v) {
@@ -126,7 +171,7 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
     return cudaErrorInvalidValue;
 }
 
-int nlm3d_fwd_variant_count(bool fp16) { return fp16 ? 3 : 4; }
+int nlm3d_fwd_variant_count(bool fp16) { return fp16 ? 3 : 6; }
 
 static bool small_case(int sr, int pr) {
 #define X_(m, n) \
@@ -148,7 +193,7 @@ size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16) {
 }
 
 int nlm3d_fwd_tile_z(int sr, int pr, bool fp16, int v) {
-    static const int f32[4] = {8, 8, 4, 8}, f16[3] = {6, 8, 8};
+    static const int f32[6] = {8, 8, 4, 8, 8, 6}, f16[3] = {6, 8, 8};
     if (v < 0 || v >= nlm3d_fwd_variant_count(fp16)) return 0;
     if (nlm3d_fwd_large_patch(sr, pr, fp16)) return nlm3d_lp_tile_z(v);
     return fp16 ? f16[v] : f32[v];

@@ -27,6 +27,8 @@
 
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "nlm_device.cuh"
 
 namespace gnlm {
@@ -237,6 +239,194 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
                 const float2 zz = zacc[r / 2][q].s, nn = nacc[r / 2][q].s;
                 const float zs = (r & 1) ? zz.y : zz.x;
                 const float nm = (r & 1) ? nn.y : nn.x;
+                out[o] = nm / zs * inv_scale;
+                if (zsum) zsum[o] = zs;
+            }
+        }
+    }
+    return true;
+}
+
+// Paired z offsets (FP32, reference values in registers): offsets (ox, oy, oz) and
+// (ox, oy, oz+1) share every candidate plane.  With c(j) the candidate plane j of
+// offset oz's stream, offset oz's difference at the thread's plane pl is
+// a(pl) - c(pl) and offset oz+1's is a(pl) - c(pl+1); streaming j = 0..PLANES, plane
+// j feeds offset oz at pl = j and offset oz+1 at pl = j-1, and the outputs they
+// complete (planes j-2N and j-1-2N) take the same candidate centre c(j-N).  Shared
+// loads per (voxel, offset): (RY+2)(RZ+2N+1) / (2 RY RZ) instead of
+// (RY+2)(RZ+2N) / (RY RZ).  2M+1 z offsets make M pairs and one single.
+template <int M, int N, int RY, int RZ, int NW>
+__device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* tile, uint64_t* bar,
+                                              uint32_t parity, int bx, int by, int bz, int X, int Y,
+                                              int Z, float inv_scale, float* __restrict__ out,
+                                              float* __restrict__ zsum, unsigned int* errword) {
+    using C = Fwd3d<M, N, float, RY, RZ, NW>;
+    static_assert(RY % 2 == 0, "rows are processed in pairs");
+    constexpr int RP = C::ROWS / 2;
+    constexpr int OP = RY / 2;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int X0 = bx * C::XO;
+    const int Y0 = by * C::TY;
+    const int Z0 = bz * RZ;
+    const int xs = X0 & ~(C::A - 1);
+    const int ral = X0 - xs;
+
+    if (threadIdx.x == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, C::TILE_BYTES);
+        tma_load_3d(tile, map, xs, Y0, Z0, bar);
+    }
+    if (!mbar_wait_bounded(bar, parity)) {
+        if (threadIdx.x == 0) {
+            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
+            mbar_wait_bounded(bar, parity);
+        }
+        return false;
+    }
+
+    const float* aptr =
+        tile + (C::H - N) * C::PLANE + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
+    float2 areg[C::PLANES][RP];
+#pragma unroll
+    for (int pl = 0; pl < C::PLANES; ++pl)
+#pragma unroll
+        for (int rp = 0; rp < RP; ++rp)
+            areg[pl][rp] = make_float2(aptr[pl * C::PLANE + (2 * rp) * C::BX],
+                                       aptr[pl * C::PLANE + (2 * rp + 1) * C::BX]);
+
+    float2 zacc[OP][RZ], nacc[OP][RZ];
+#pragma unroll
+    for (int r = 0; r < OP; ++r)
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) zacc[r][q] = nacc[r][q] = make_float2(0.f, 0.f);
+    const float2 minus1 = make_float2(-1.f, -1.f);
+
+    // y box, x box, weight and accumulation of output plane q from the z-window sums S
+    // of rows 0..ROWS-1, with candidate centres cc (rows N..N+RY-1).
+    auto emit = [&](const float2 (&S)[RP], const int q, const float (&cc)[RY]) {
+        float Srow[C::ROWS];
+#pragma unroll
+        for (int rp = 0; rp < RP; ++rp) {
+            Srow[2 * rp] = S[rp].x;
+            Srow[2 * rp + 1] = S[rp].y;
+        }
+        float Yv[RY];
+        if constexpr (N == 1) {
+#pragma unroll
+            for (int r = 0; r < RY; r += 2) {
+                const float u = Srow[r + 1] + Srow[r + 2];
+                Yv[r] = Srow[r] + u;
+                Yv[r + 1] = u + Srow[r + 3];
+            }
+        } else {
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < C::K; ++k) acc += Srow[k];
+            Yv[0] = acc;
+#pragma unroll
+            for (int r = 1; r < RY; ++r) {
+                acc = acc + Srow[r + C::K - 1] - Srow[r - 1];
+                Yv[r] = acc;
+            }
+        }
+#pragma unroll
+        for (int op = 0; op < OP; ++op) {
+            float2 xv = make_float2(Yv[2 * op], Yv[2 * op + 1]);
+#pragma unroll
+            for (int k = 1; k <= N; ++k) {
+                const float2 dn = make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], k),
+                                              __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], k));
+                const float2 up = make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], k),
+                                              __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], k));
+                xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
+            }
+            const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
+            zacc[op][q] = __fadd2_rn(zacc[op][q], w);
+            nacc[op][q] = __ffma2_rn(w, make_float2(cc[2 * op], cc[2 * op + 1]), nacc[op][q]);
+        }
+    };
+
+    auto zpair = [&](const float* bptr, auto second_tag) {
+        constexpr bool SECOND = decltype(second_tag)::value;
+        constexpr int JEND = SECOND ? C::PLANES + 1 : C::PLANES;
+        float2 S0[RP], S1[RP];
+        float2 tr0[C::K][RP], tr1[C::K][RP];
+        float cand[N + 1][RY];
+#pragma unroll
+        for (int j = 0; j < JEND; ++j) {
+            float2 c2[RP];
+#pragma unroll
+            for (int rp = 0; rp < RP; ++rp) {
+                const float b0 = bptr[j * C::PLANE + (2 * rp) * C::BX];
+                const float b1 = bptr[j * C::PLANE + (2 * rp + 1) * C::BX];
+                c2[rp] = make_float2(b0, b1);
+                const int r0 = 2 * rp, r1 = 2 * rp + 1;
+                if (r0 >= N && r0 < RY + N) cand[j % (N + 1)][r0 - N] = b0;
+                if (r1 >= N && r1 < RY + N) cand[j % (N + 1)][r1 - N] = b1;
+            }
+            if (j < C::PLANES) {  // offset oz, thread plane j
+                const int pl = j;
+#pragma unroll
+                for (int rp = 0; rp < RP; ++rp) {
+                    const float2 t = __ffma2_rn(c2[rp], minus1, areg[pl][rp]);
+                    if (pl == 0)
+                        S0[rp] = __fmul2_rn(t, t);
+                    else
+                        S0[rp] = __ffma2_rn(t, t, S0[rp]);
+                    if (pl >= C::K) {
+                        const float2 to = tr0[(pl - C::K) % C::K][rp];
+                        S0[rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S0[rp]);
+                    }
+                    tr0[pl % C::K][rp] = t;
+                }
+                if (pl >= 2 * N) emit(S0, pl - 2 * N, cand[(j - N) % (N + 1)]);
+            }
+            if constexpr (SECOND) {
+                if (j >= 1) {  // offset oz+1, thread plane j-1
+                    const int pl = j - 1;
+#pragma unroll
+                    for (int rp = 0; rp < RP; ++rp) {
+                        const float2 t = __ffma2_rn(c2[rp], minus1, areg[pl][rp]);
+                        if (pl == 0)
+                            S1[rp] = __fmul2_rn(t, t);
+                        else
+                            S1[rp] = __ffma2_rn(t, t, S1[rp]);
+                        if (pl >= C::K) {
+                            const float2 to = tr1[(pl - C::K) % C::K][rp];
+                            S1[rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S1[rp]);
+                        }
+                        tr1[pl % C::K][rp] = t;
+                    }
+                    if (pl >= 2 * N) emit(S1, pl - 2 * N, cand[(j - N) % (N + 1)]);
+                }
+            }
+        }
+    };
+
+    for (int oy = -M; oy <= M; ++oy) {
+        for (int ox = -M; ox <= M; ++ox) {
+            const float* bxy = aptr + oy * C::BX + ox;
+            for (int oz = -M; oz < M; oz += 2)
+                zpair(bxy + oz * C::PLANE, std::integral_constant<bool, true>());
+            zpair(bxy + M * C::PLANE, std::integral_constant<bool, false>());
+        }
+    }
+
+    const int x = X0 + lane - N;
+    if (lane >= N && lane < 32 - N && x < X) {
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) {
+            const int z = Z0 + q;
+            if (z >= Z) break;
+#pragma unroll
+            for (int r = 0; r < RY; ++r) {
+                const int y = Y0 + warp * RY + r;
+                if (y >= Y) break;
+                const size_t o = ((size_t)z * Y + y) * X + x;
+                const float zs = (r & 1) ? zacc[r / 2][q].y : zacc[r / 2][q].x;
+                const float nm = (r & 1) ? nacc[r / 2][q].y : nacc[r / 2][q].x;
                 out[o] = nm / zs * inv_scale;
                 if (zsum) zsum[o] = zs;
             }
