@@ -26,8 +26,8 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                                                   errword);
 }
 
-// Single-volume kernel with paired z offsets (fwd3d_tile_pz).
-template <int M, int N, int RY, int RZ, int NW, int MINB>
+// Single-volume kernel with grouped z offsets (fwd3d_tile_pz).
+template <int M, int N, int RY, int RZ, int NW, int MINB, int GZ>
 __global__ void __launch_bounds__(32 * NW, MINB)
     nlm3d_fwd_pz_kernel(const __grid_constant__ CUtensorMap tmap, int X, int Y, int Z,
                         float inv_scale, float* __restrict__ out, float* __restrict__ zsum,
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         fence_mbar_init();
     }
     __syncthreads();
-    fwd3d_tile_pz<M, N, RY, RZ, NW>(&tmap, tile, bar, 0, blockIdx.x, blockIdx.y, blockIdx.z + bz0,
+    fwd3d_tile_pz<M, N, RY, RZ, NW, GZ>(&tmap, tile, bar, 0, blockIdx.x, blockIdx.y, blockIdx.z + bz0,
                                     X, Y, Z, inv_scale, out, zsum, errword);
 }
 
@@ -90,7 +90,7 @@ static cudaError_t run_fwd3d_h2(const Staging& st, const void* staged, float inv
     return cudaGetLastError();
 }
 
-template <int M, int N, int RY, int RZ, int NW, int MINB>
+template <int M, int N, int RY, int RZ, int NW, int MINB, int GZ>
 static cudaError_t run_fwd3d_pz(const Staging& st, const void* staged, float inv_scale, float* out,
                                 float* zsum, unsigned int* errword, cudaStream_t stream, int zt0,
                                 int zt1) {
@@ -101,7 +101,7 @@ static cudaError_t run_fwd3d_pz(const Staging& st, const void* staged, float inv
     const uint32_t box[3] = {(uint32_t)C::BX, (uint32_t)C::BY, (uint32_t)C::BZ};
     cudaError_t e = encode_tensor_map(&map, false, 3, dims, strides, box, const_cast<void*>(staged));
     if (e != cudaSuccess) return e;
-    auto kern = nlm3d_fwd_pz_kernel<M, N, RY, RZ, NW, MINB>;
+    auto kern = nlm3d_fwd_pz_kernel<M, N, RY, RZ, NW, MINB, GZ>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     if (zt1 < 0) zt1 = (st.Z + RZ - 1) / RZ;
@@ -145,7 +145,8 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
 //   2: 4 x 4, registers, 3 CTAs/SM
 //   3: 2 x 8, registers, 3 CTAs/SM
 //   4: 4 x 8, registers, z offsets in pairs sharing candidate planes, 2 CTAs/SM
-//   5: 4 x 6, as 4
+//   5: 4 x 6, z offsets in groups of three, 2 CTAs/SM
+//   6: 4 x 8, groups of three, 2 CTAs/SM
 // FP16-storage form (row-pair layout, Kahan-compensated weight sum):
 //   0: 4 x 6, 2 CTAs/SM;  1: 4 x 8, 2 CTAs/SM;  2: 2 x 8, 3 CTAs/SM
 template <int m, int n>
@@ -158,8 +159,9 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
             case 1: return run_fwd3d<m, n, float, 4, 8, 4, 3, false, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 2: return run_fwd3d<m, n, float, 4, 4, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 3: return run_fwd3d<m, n, float, 2, 8, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
-            case 4: return run_fwd3d_pz<m, n, 4, 8, 4, 2>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
-            case 5: return run_fwd3d_pz<m, n, 4, 6, 4, 2>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 4: return run_fwd3d_pz<m, n, 4, 8, 4, 2, 2>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 5: return run_fwd3d_pz<m, n, 4, 6, 4, 2, 3>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 6: return run_fwd3d_pz<m, n, 4, 8, 4, 2, 3>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
         }
     } else {
         switch (v) {
@@ -171,7 +173,7 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
     return cudaErrorInvalidValue;
 }
 
-int nlm3d_fwd_variant_count(bool fp16) { return fp16 ? 3 : 6; }
+int nlm3d_fwd_variant_count(bool fp16) { return fp16 ? 3 : 7; }
 
 static bool small_case(int sr, int pr) {
 #define X_(m, n) \
@@ -193,7 +195,7 @@ size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16) {
 }
 
 int nlm3d_fwd_tile_z(int sr, int pr, bool fp16, int v) {
-    static const int f32[6] = {8, 8, 4, 8, 8, 6}, f16[3] = {6, 8, 8};
+    static const int f32[7] = {8, 8, 4, 8, 8, 6, 8}, f16[3] = {6, 8, 8};
     if (v < 0 || v >= nlm3d_fwd_variant_count(fp16)) return 0;
     if (nlm3d_fwd_large_patch(sr, pr, fp16)) return nlm3d_lp_tile_z(v);
     return fp16 ? f16[v] : f32[v];

@@ -52,9 +52,9 @@ static cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     X_(6, 1) X_(1, 2) X_(2, 2) X_(4, 2) X_(6, 2)
 
 // Chunk depth per variant (planes streamed per CTA).
-static const int kLpTz[6] = {64, 32, 128, 16, 48, 96};
+static const int kLpTz[7] = {64, 32, 128, 16, 48, 96, 80};
 
-int nlm3d_lp_tile_z(int variant) { return (variant >= 0 && variant < 6) ? kLpTz[variant] : 0; }
+int nlm3d_lp_tile_z(int variant) { return (variant >= 0 && variant < 7) ? kLpTz[variant] : 0; }
 
 bool nlm3d_lp_supported(int sr, int pr) {
 #define X_(m, n) \

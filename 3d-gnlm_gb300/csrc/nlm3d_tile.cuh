@@ -247,15 +247,15 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
     return true;
 }
 
-// Paired z offsets (FP32, reference values in registers): offsets (ox, oy, oz) and
-// (ox, oy, oz+1) share every candidate plane.  With c(j) the candidate plane j of
-// offset oz's stream, offset oz's difference at the thread's plane pl is
-// a(pl) - c(pl) and offset oz+1's is a(pl) - c(pl+1); streaming j = 0..PLANES, plane
-// j feeds offset oz at pl = j and offset oz+1 at pl = j-1, and the outputs they
-// complete (planes j-2N and j-1-2N) take the same candidate centre c(j-N).  Shared
-// loads per (voxel, offset): (RY+2)(RZ+2N+1) / (2 RY RZ) instead of
-// (RY+2)(RZ+2N) / (RY RZ).  2M+1 z offsets make M pairs and one single.
-template <int M, int N, int RY, int RZ, int NW>
+// Grouped z offsets (FP32, reference values in registers): the GZ offsets
+// (ox, oy, oz+g), g < GZ, share every candidate plane.  With c(j) the candidate plane
+// j of offset oz's stream, offset oz+g's difference at the thread's plane pl is
+// a(pl) - c(pl+g); streaming j = 0..PLANES+GZ-2, plane j feeds offset oz+g at
+// pl = j-g, and every output a member completes at that step (plane j-g-2N) takes
+// the same candidate centre c(j-N).  Shared loads per (voxel, offset):
+// (RY+2)(RZ+2N+GZ-1) / (GZ RY RZ) instead of (RY+2)(RZ+2N) / (RY RZ).  The 2M+1 z
+// offsets make (2M+1)/GZ full groups and one shorter group for the rest.
+template <int M, int N, int RY, int RZ, int NW, int GZ>
 __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* tile, uint64_t* bar,
                                               uint32_t parity, int bx, int by, int bz, int X, int Y,
                                               int Z, float inv_scale, float* __restrict__ out,
@@ -348,11 +348,11 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
         }
     };
 
-    auto zpair = [&](const float* bptr, auto second_tag) {
-        constexpr bool SECOND = decltype(second_tag)::value;
-        constexpr int JEND = SECOND ? C::PLANES + 1 : C::PLANES;
-        float2 S0[RP], S1[RP];
-        float2 tr0[C::K][RP], tr1[C::K][RP];
+    auto zgroup = [&](const float* bptr, auto size_tag) {
+        constexpr int G = decltype(size_tag)::value;
+        constexpr int JEND = C::PLANES + G - 1;
+        float2 S[G][RP];
+        float2 tr[G][C::K][RP];
         float cand[N + 1][RY];
 #pragma unroll
         for (int j = 0; j < JEND; ++j) {
@@ -366,51 +366,38 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
                 if (r0 >= N && r0 < RY + N) cand[j % (N + 1)][r0 - N] = b0;
                 if (r1 >= N && r1 < RY + N) cand[j % (N + 1)][r1 - N] = b1;
             }
-            if (j < C::PLANES) {  // offset oz, thread plane j
-                const int pl = j;
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int pl = j - g;  // offset oz+g, thread plane pl
+                if (pl < 0 || pl >= C::PLANES) continue;
 #pragma unroll
                 for (int rp = 0; rp < RP; ++rp) {
                     const float2 t = __ffma2_rn(c2[rp], minus1, areg[pl][rp]);
                     if (pl == 0)
-                        S0[rp] = __fmul2_rn(t, t);
+                        S[g][rp] = __fmul2_rn(t, t);
                     else
-                        S0[rp] = __ffma2_rn(t, t, S0[rp]);
+                        S[g][rp] = __ffma2_rn(t, t, S[g][rp]);
                     if (pl >= C::K) {
-                        const float2 to = tr0[(pl - C::K) % C::K][rp];
-                        S0[rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S0[rp]);
+                        const float2 to = tr[g][(pl - C::K) % C::K][rp];
+                        S[g][rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S[g][rp]);
                     }
-                    tr0[pl % C::K][rp] = t;
+                    tr[g][pl % C::K][rp] = t;
                 }
-                if (pl >= 2 * N) emit(S0, pl - 2 * N, cand[(j - N) % (N + 1)]);
-            }
-            if constexpr (SECOND) {
-                if (j >= 1) {  // offset oz+1, thread plane j-1
-                    const int pl = j - 1;
-#pragma unroll
-                    for (int rp = 0; rp < RP; ++rp) {
-                        const float2 t = __ffma2_rn(c2[rp], minus1, areg[pl][rp]);
-                        if (pl == 0)
-                            S1[rp] = __fmul2_rn(t, t);
-                        else
-                            S1[rp] = __ffma2_rn(t, t, S1[rp]);
-                        if (pl >= C::K) {
-                            const float2 to = tr1[(pl - C::K) % C::K][rp];
-                            S1[rp] = __ffma2_rn(make_float2(-to.x, -to.y), to, S1[rp]);
-                        }
-                        tr1[pl % C::K][rp] = t;
-                    }
-                    if (pl >= 2 * N) emit(S1, pl - 2 * N, cand[(j - N) % (N + 1)]);
-                }
+                if (pl >= 2 * N) emit(S[g], pl - 2 * N, cand[(j - N) % (N + 1)]);
             }
         }
     };
 
+    constexpr int NZ = 2 * M + 1;
+    constexpr int REM = NZ % GZ;
     for (int oy = -M; oy <= M; ++oy) {
         for (int ox = -M; ox <= M; ++ox) {
             const float* bxy = aptr + oy * C::BX + ox;
-            for (int oz = -M; oz < M; oz += 2)
-                zpair(bxy + oz * C::PLANE, std::integral_constant<bool, true>());
-            zpair(bxy + M * C::PLANE, std::integral_constant<bool, false>());
+#pragma unroll 1
+            for (int oz = -M; oz + GZ - 1 <= M; oz += GZ)
+                zgroup(bxy + oz * C::PLANE, std::integral_constant<int, GZ>());
+            if constexpr (REM > 0)
+                zgroup(bxy + (M - REM + 1) * C::PLANE, std::integral_constant<int, REM>());
         }
     }
 
