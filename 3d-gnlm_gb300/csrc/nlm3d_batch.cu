@@ -14,8 +14,9 @@
 //   * graph = [zero the work counter] -> [batched staging] -> [persistent kernel].
 // The persistent kernel runs (occupancy x SMs) CTAs; each CTA takes the next work
 // item with one atomicAdd (no waiting: an index past the end means done), loads the
-// item's tile with TMA on its mbarrier (the phase flips per item) and runs the same
-// per-tile body as the single-volume kernel.  The tile shape is a template
+// item's tile with TMA on its mbarrier (the phase flips per item) and runs the
+// single-volume kernel's tile body with z offsets in groups of three
+// (fwd3d_tile_pz in nlm3d_tile.cuh).  The tile shape is a template
 // parameter; the plan's autotuner times each shape on the batch and keeps the
 // fastest.
 #include <stdio.h>
@@ -116,10 +117,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         switch (v->sr) {
 #define X_(m)                                                                                     \
     case m:                                                                                       \
-        ok = fwd3d_tile<m, 1, float, RY, RZ, NW, true, false>(&v->map, tile, bar, k & 1u, item.y,  \
-                                                              item.z, item.w, v->X, v->Y, v->Z, \
-                                                              v->inv_scale, v->out, v->zsum,    \
-                                                              errword);                         \
+        ok = fwd3d_tile_pz<m, 1, RY, RZ, NW, 3>(&v->map, tile, bar, k & 1u, item.y, item.z,      \
+                                                 item.w, v->X, v->Y, v->Z, v->inv_scale, v->out,   \
+                                                 v->zsum, errword);                                \
         break;
             GNLM_BATCH_RADII(X_)
 #undef X_
