@@ -464,7 +464,9 @@ def run_gnlm(args):
     large = bench_large_patch(torch, gnlm) if not args.skip_extra else None
     fused_mean = statistics.mean(fused_ms)
     achieved = FLOPS_PER_PAIR * OFFSETS * nvox / (fused_mean * 1e-3) / 1e12
-    traffic = read_profile_traffic("nlm3d_fwd_kernel")
+    # FP32 variants 4-6 are the grouped-z kernel, 0-3 the one-offset-at-a-time kernel
+    kname = "nlm3d_fwd_pz_kernel" if tuned32[0] >= 4 else "nlm3d_fwd_kernel"
+    traffic = read_profile_traffic(kname)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
@@ -480,7 +482,7 @@ def run_gnlm(args):
                      "peak": round(peak, 3), "unit": "TFLOP/s",
                      "frac": round(achieved / peak, 4) if peak else None,
                      "traffic": traffic,
-                     "kernel": f"nlm3d_fwd_kernel<3,1,float> variant {tuned32[0]}",
+                     "kernel": f"{kname}<3,1> (FP32 variant {tuned32[0]})",
                      "peak_source": "FFMA probe kernel measured in this run (FP32 pipe; "
                                     "MEASURED_PEAKS.json has HBM and bf16 only)",
                      "algorithmic": f"{FLOPS_PER_PAIR} flops x {OFFSETS} offsets x {nvox} voxels"},
