@@ -15,6 +15,8 @@
 // add/sub per axis, scale, weight-sum add, weighted-value FMA) + 1 exp.
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "nlm_device.cuh"
 #include "nlm_internal.h"
 
@@ -41,12 +43,17 @@ struct Fwd2d {
     static_assert(BAR_OFF % 128 == 0, "the tile (at offset 0) and barrier stay 128-byte aligned");
 };
 
-// Sum of y over the lanes [l - N, l + N] (valid for lanes N .. 31 - N).  Up to
-// N = 2 two shuffles per radius step; wider windows are assembled from
+// Sum of y over the lanes [l - N, l + N] (valid for lanes N .. 31 - N).  N = 1: two
+// shuffles; N = 2: three (from pair sums); wider windows are assembled from
 // power-of-two window sums, e.g. 11 = 8 + 2 + 1 takes 6 shuffles instead of 10.
 template <int N>
 __device__ __forceinline__ float xbox_lanes(float y) {
-    if constexpr (N <= 2) {
+    if constexpr (N == 2) {
+        // P = y(l) + y(l+1); box = P(l-2) + P(l) + y(l+2): three shuffles
+        const float yr = __shfl_down_sync(0xffffffffu, y, 1);
+        const float p = y + yr;
+        return __shfl_up_sync(0xffffffffu, p, 2) + p + __shfl_down_sync(0xffffffffu, y, 2);
+    } else if constexpr (N <= 2) {
         float x = y;
 #pragma unroll
         for (int k = 1; k <= N; ++k)
@@ -76,7 +83,10 @@ __device__ __forceinline__ float xbox_lanes(float y) {
 
 // Thread = one column (lane) x RY rows; the reference rows sit in registers
 // for all offsets; rows are processed in pairs as packed FP32x2 arithmetic.
-template <int M, int N, typename T, int RY, int NW, int MINB>
+// G > 1: the y offsets (ox, oy+g), g < G, share one pass over the candidate rows
+// (offset oy+g's candidate for thread row r is row r+g of offset oy's), so candidate
+// loads per (pixel, offset) drop from (RY+2N)/RY to (RY+2N+G-1)/(G RY).
+template <int M, int N, typename T, int RY, int NW, int MINB, int G>
 __global__ void __launch_bounds__(32 * NW, MINB)
     nlm2d_fwd_kernel(const __grid_constant__ CUtensorMap tmap, int X, int Y, float inv_scale,
                      float* __restrict__ out, float* __restrict__ zsum, unsigned int* errword) {
@@ -122,6 +132,62 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     for (int r = 0; r < OP; ++r) zacc[r] = nacc[r] = make_float2(0.f, 0.f);
     const float2 minus1 = make_float2(-1.f, -1.f);
 
+    if constexpr (G > 1) {
+        auto group = [&](const T* bptr, auto size_tag) {
+            constexpr int GG = decltype(size_tag)::value;
+            float c[C::ROWS + GG - 1];
+#pragma unroll
+            for (int j = 0; j < C::ROWS + GG - 1; ++j) c[j] = to_f32(bptr[j * C::BX]);
+#pragma unroll
+            for (int g = 0; g < GG; ++g) {
+                float q[C::ROWS];
+#pragma unroll
+                for (int rp = 0; rp < RP; ++rp) {
+                    const float2 t = __ffma2_rn(make_float2(c[2 * rp + g], c[2 * rp + 1 + g]), minus1,
+                                                areg[rp]);
+                    const float2 t2 = __fmul2_rn(t, t);
+                    q[2 * rp] = t2.x;
+                    q[2 * rp + 1] = t2.y;
+                }
+                float Yv[RY];
+                if constexpr (N == 1) {
+#pragma unroll
+                    for (int r = 0; r < RY; r += 2) {
+                        const float u = q[r + 1] + q[r + 2];
+                        Yv[r] = q[r] + u;
+                        Yv[r + 1] = u + q[r + 3];
+                    }
+                } else {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int k = 0; k < C::K; ++k) acc += q[k];
+                    Yv[0] = acc;
+#pragma unroll
+                    for (int r = 1; r < RY; ++r) {
+                        acc = acc + q[r + 2 * N] - q[r - 1];
+                        Yv[r] = acc;
+                    }
+                }
+#pragma unroll
+                for (int op = 0; op < OP; ++op) {
+                    const float x0 = xbox_lanes<N>(Yv[2 * op]);
+                    const float x1 = xbox_lanes<N>(Yv[2 * op + 1]);
+                    const float2 w = make_float2(ex2_neg(x0), ex2_neg(x1));
+                    zacc[op] = __fadd2_rn(zacc[op], w);
+                    nacc[op] = __ffma2_rn(
+                        w, make_float2(c[2 * op + N + g], c[2 * op + 1 + N + g]), nacc[op]);
+                }
+            }
+        };
+        constexpr int REM = (2 * M + 1) % G;
+        for (int ox = -M; ox <= M; ++ox) {
+#pragma unroll 1
+            for (int oy = -M; oy + G - 1 <= M; oy += G)
+                group(aptr + oy * C::BX + ox, std::integral_constant<int, G>());
+            if constexpr (REM > 0)
+                group(aptr + (M - REM + 1) * C::BX + ox, std::integral_constant<int, REM>());
+        }
+    } else
     for (int oy = -M; oy <= M; ++oy) {
         for (int ox = -M; ox <= M; ++ox) {
             const T* bptr = aptr + oy * C::BX + ox;
@@ -181,7 +247,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
 }
 
-template <int M, int N, typename T, int RY, int NW, int MINB>
+template <int M, int N, typename T, int RY, int NW, int MINB, int G = 1>
 static cudaError_t run_fwd2d(const Staging& st, const void* staged, float inv_scale, float* out,
                              float* zsum, unsigned int* errword, cudaStream_t stream) {
     using C = Fwd2d<M, N, T, RY, NW>;
@@ -192,7 +258,7 @@ static cudaError_t run_fwd2d(const Staging& st, const void* staged, float inv_sc
     cudaError_t e = encode_tensor_map(&map, sizeof(T) == 2, 2, dims, strides, box,
                                       const_cast<void*>(staged));
     if (e != cudaSuccess) return e;
-    auto kern = nlm2d_fwd_kernel<M, N, T, RY, NW, MINB>;
+    auto kern = nlm2d_fwd_kernel<M, N, T, RY, NW, MINB, G>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     dim3 grid((st.X + C::XO - 1) / C::XO, (st.Y + C::TY - 1) / C::TY);
@@ -206,7 +272,8 @@ static cudaError_t run_fwd2d(const Staging& st, const void* staged, float inv_sc
 #define GNLM_FWD2D_CASES(X_) \
     X_(1, 1) X_(3, 1) X_(5, 1) X_(3, 2) X_(5, 2) X_(7, 2) X_(3, 5) X_(7, 5) X_(10, 5)
 
-// Tile variants: 0: 16 rows per thread, 4 warps; 1: 8 rows, 4 warps; 2: 16 rows, 8 warps.
+// Tile variants: 0: 16 rows per thread, 4 warps; 1: 8 rows, 4 warps; 2: 16 rows, 8 warps;
+// 3, 4: as 0 and 2 with y offsets in groups of three.
 template <int m, int n>
 static cudaError_t run2d_variant(const Staging& st, const void* staged, bool fp16, int v,
                                  float inv_scale, float* out, float* zsum, unsigned int* ew,
@@ -216,18 +283,22 @@ static cudaError_t run2d_variant(const Staging& st, const void* staged, bool fp1
             case 0: return run_fwd2d<m, n, __half, 16, 4, 3>(st, staged, inv_scale, out, zsum, ew, s);
             case 1: return run_fwd2d<m, n, __half, 8, 4, 4>(st, staged, inv_scale, out, zsum, ew, s);
             case 2: return run_fwd2d<m, n, __half, 16, 8, 2>(st, staged, inv_scale, out, zsum, ew, s);
+            case 3: return run_fwd2d<m, n, __half, 16, 4, 3, 3>(st, staged, inv_scale, out, zsum, ew, s);
+            case 4: return run_fwd2d<m, n, __half, 16, 8, 2, 3>(st, staged, inv_scale, out, zsum, ew, s);
         }
     } else {
         switch (v) {
             case 0: return run_fwd2d<m, n, float, 16, 4, 3>(st, staged, inv_scale, out, zsum, ew, s);
             case 1: return run_fwd2d<m, n, float, 8, 4, 4>(st, staged, inv_scale, out, zsum, ew, s);
             case 2: return run_fwd2d<m, n, float, 16, 8, 2>(st, staged, inv_scale, out, zsum, ew, s);
+            case 3: return run_fwd2d<m, n, float, 16, 4, 3, 3>(st, staged, inv_scale, out, zsum, ew, s);
+            case 4: return run_fwd2d<m, n, float, 16, 8, 2, 3>(st, staged, inv_scale, out, zsum, ew, s);
         }
     }
     return cudaErrorInvalidValue;
 }
 
-int nlm2d_fwd_variant_count() { return 3; }
+int nlm2d_fwd_variant_count() { return 5; }
 
 bool nlm2d_fwd_supported(int sr, int pr, bool fp16) {
     (void)fp16;
