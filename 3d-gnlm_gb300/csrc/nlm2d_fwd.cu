@@ -43,44 +43,6 @@ struct Fwd2d {
     static_assert(BAR_OFF % 128 == 0, "the tile (at offset 0) and barrier stay 128-byte aligned");
 };
 
-// Sum of y over the lanes [l - N, l + N] (valid for lanes N .. 31 - N).  N = 1: two
-// shuffles; N = 2: three (from pair sums); wider windows are assembled from
-// power-of-two window sums, e.g. 11 = 8 + 2 + 1 takes 6 shuffles instead of 10.
-template <int N>
-__device__ __forceinline__ float xbox_lanes(float y) {
-    if constexpr (N == 2) {
-        // P = y(l) + y(l+1); box = P(l-2) + P(l) + y(l+2): three shuffles
-        const float yr = __shfl_down_sync(0xffffffffu, y, 1);
-        const float p = y + yr;
-        return __shfl_up_sync(0xffffffffu, p, 2) + p + __shfl_down_sync(0xffffffffu, y, 2);
-    } else if constexpr (N <= 2) {
-        float x = y;
-#pragma unroll
-        for (int k = 1; k <= N; ++k)
-            x += __shfl_down_sync(0xffffffffu, y, k) + __shfl_up_sync(0xffffffffu, y, k);
-        return x;
-    } else {
-        constexpr int K = 2 * N + 1;
-        float p[5];  // p[j] = sum over lanes l .. l + 2^j - 1
-        p[0] = y;
-#pragma unroll
-        for (int j = 1; j < 5; ++j)
-            p[j] = (1 << j) <= K ? p[j - 1] + __shfl_down_sync(0xffffffffu, p[j - 1], 1 << (j - 1))
-                                 : 0.f;
-        float x = 0.f;
-        int start = -N;  // window start relative to this lane
-#pragma unroll
-        for (int j = 4; j >= 0; --j) {
-            if (K & (1 << j)) {
-                x += start < 0 ? __shfl_up_sync(0xffffffffu, p[j], -start)
-                               : (start == 0 ? p[j] : __shfl_down_sync(0xffffffffu, p[j], start));
-                start += 1 << j;
-            }
-        }
-        return x;
-    }
-}
-
 // Thread = one column (lane) x RY rows; the reference rows sit in registers
 // for all offsets; rows are processed in pairs as packed FP32x2 arithmetic.
 // G > 1: the y offsets (ox, oy+g), g < G, share one pass over the candidate rows

@@ -209,12 +209,7 @@ __global__ void __launch_bounds__(32 * NW, 1)
                 for (int r = 0; r < C::RD; ++r)
 #pragma unroll
                     for (int p = 0; p < C::PD; ++p) {
-                        const float yv = D[r][p];
-                        float xv = yv;
-#pragma unroll
-                        for (int k = 1; k <= N; ++k)
-                            xv += __shfl_down_sync(0xffffffffu, yv, k) + __shfl_up_sync(0xffffffffu, yv, k);
-                        D[r][p] = xv;
+                        D[r][p] = xbox_lanes<N>(D[r][p]);
                     }
                 // weights, G(u+o), and the field a_o(u) (without the -ln2)
                 float e[C::RD][C::PD], a[C::RD][C::PD], guo[C::RD][C::PD];
@@ -247,10 +242,7 @@ __global__ void __launch_bounds__(32 * NW, 1)
                         float yv = za[r][q];
 #pragma unroll
                         for (int ky = 1; ky < C::K; ++ky) yv += za[r + ky][q];
-                        float xv = yv;
-#pragma unroll
-                        for (int k = 1; k <= N; ++k)
-                            xv += __shfl_down_sync(0xffffffffu, yv, k) + __shfl_up_sync(0xffffffffu, yv, k);
+                        const float xv = xbox_lanes<N>(yv);
                         // gpad' += G(q+o) e_q(o) + 2 (v'_q - v'_{q+o}) (-ln2) A(q)
                         acc[r][q] = fmaf(guo[r + N][q + N], e[r + N][q + N], acc[r][q]);
                         acc[r][q] = fmaf(-2.f * kLn2 * ts(r + 2 * N, q + 2 * N), xv, acc[r][q]);

@@ -198,15 +198,16 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
 #pragma unroll
                         for (int op = 0; op < OP; ++op) {
                             float2 xv = make_float2(Yv[2 * op], Yv[2 * op + 1]);
-#pragma unroll
-                            for (int k = 1; k <= N; ++k) {
+                            if constexpr (N == 1) {
                                 const float2 dn =
-                                    make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], k),
-                                                __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                    make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], 1),
+                                                __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], 1));
                                 const float2 up =
-                                    make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], k),
-                                                __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                    make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], 1),
+                                                __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], 1));
                                 xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
+                            } else {
+                                xv = make_float2(xbox_lanes<N>(Yv[2 * op]), xbox_lanes<N>(Yv[2 * op + 1]));
                             }
                             const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
                             const float2 c = make_float2(cand[(pl - N) % (N + 1)][2 * op],
@@ -334,13 +335,14 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
 #pragma unroll
         for (int op = 0; op < OP; ++op) {
             float2 xv = make_float2(Yv[2 * op], Yv[2 * op + 1]);
-#pragma unroll
-            for (int k = 1; k <= N; ++k) {
-                const float2 dn = make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], k),
-                                              __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], k));
-                const float2 up = make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], k),
-                                              __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], k));
+            if constexpr (N == 1) {
+                const float2 dn = make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], 1),
+                                              __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], 1));
+                const float2 up = make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], 1),
+                                              __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], 1));
                 xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
+            } else {
+                xv = make_float2(xbox_lanes<N>(Yv[2 * op]), xbox_lanes<N>(Yv[2 * op + 1]));
             }
             const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
             zacc[op][q] = __fadd2_rn(zacc[op][q], w);
@@ -587,15 +589,16 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
 #pragma unroll
                         for (int op = 0; op < OP; ++op) {
                             float2 xv = make_float2(Yv[2 * op], Yv[2 * op + 1]);
-#pragma unroll
-                            for (int k = 1; k <= N; ++k) {
+                            if constexpr (N == 1) {
                                 const float2 dn =
-                                    make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], k),
-                                                __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                    make_float2(__shfl_down_sync(0xffffffffu, Yv[2 * op], 1),
+                                                __shfl_down_sync(0xffffffffu, Yv[2 * op + 1], 1));
                                 const float2 up =
-                                    make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], k),
-                                                __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], k));
+                                    make_float2(__shfl_up_sync(0xffffffffu, Yv[2 * op], 1),
+                                                __shfl_up_sync(0xffffffffu, Yv[2 * op + 1], 1));
                                 xv = __fadd2_rn(xv, __fadd2_rn(dn, up));
+                            } else {
+                                xv = make_float2(xbox_lanes<N>(Yv[2 * op]), xbox_lanes<N>(Yv[2 * op + 1]));
                             }
                             const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
                             zrun[op][q] = __fadd2_rn(zrun[op][q], w);

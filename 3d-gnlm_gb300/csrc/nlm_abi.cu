@@ -154,10 +154,25 @@ int check_dims3(int X, int Y, int Z, int H) {
 
 int report_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
+// Variant used before any autotuning: the fastest measured on a GB300 for the
+// configuration family (3D FP32 patch 3: z offsets in groups of three, 4 x 8;
+// search 11 / patch 5: groups of three, 4 x 6; 2D FP32: y offsets in groups of
+// three, 8 warps for patch 11 and wider), else variant 0.
+int default_variant(int dims, int sr, int pr, bool fp16) {
+    if (fp16) return 0;
+    if (dims == 3) {
+        if (nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
+        if (pr == 1) return 6;
+        if (pr == 2 && sr == 5) return 5;
+        return 0;
+    }
+    return pr >= 5 ? 4 : 3;
+}
+
 int tuned_variant(int dims, int sr, int pr, bool fp16) {
     std::lock_guard<std::mutex> lk(g_mutex);
     auto it = g_tuned.find(tune_key(dims, sr, pr, fp16));
-    return it == g_tuned.end() ? 0 : it->second;
+    return it == g_tuned.end() ? default_variant(dims, sr, pr, fp16) : it->second;
 }
 
 unsigned int* device_error_word() {

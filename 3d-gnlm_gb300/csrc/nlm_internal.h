@@ -83,8 +83,9 @@ cudaError_t launch_nlm3d_adj(const Staging& st, const void* staged, const float*
                              double* hpart, unsigned int* errword, cudaStream_t stream);
 
 // Tile-shape variant the forward uses for (dims, sr, pr, fp16): the autotuned
-// choice if one was recorded, else 0.
+// choice if one was recorded, else default_variant().
 int tuned_variant(int dims, int sr, int pr, bool fp16);
+int default_variant(int dims, int sr, int pr, bool fp16);
 
 // 2D forward over a staged image (Z = 1, Hz = 0).
 cudaError_t launch_nlm2d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,

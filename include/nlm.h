@@ -193,7 +193,9 @@ int nlm3d_batch_destroy(nlm_batch_plan* plan);
 /*
  * Tile-shape variants of the fused kernels (no counterpart in the reference,
  * whose block/grid shape is fixed by macros, 3DNLM/main.cu:15-21).  Forward calls
- * use the recorded variant for (dims, sr, pr, FP16 flag), or variant 0.
+ * use the recorded variant for (dims, sr, pr, FP16 flag), or, when none is
+ * recorded (or after a reset with -1), a per-configuration default measured on a
+ * GB300; nlm_get_variant reports whichever applies.
  */
 int nlm_variant_count(int dims, unsigned int flags);
 int nlm_set_variant(int dims, int sr, int pr, unsigned int flags, int variant); /* -1 = reset */

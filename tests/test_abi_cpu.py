@@ -116,3 +116,18 @@ def test_2d_rejects_bad_arguments(L):
     rc = L.nlm2d_forward(ctypes.c_void_p(1), gnlm.NLM_F32, 8, 8, 4, 4, 0.08, ctypes.c_void_p(1),
                          None, 0, None, 0, None)
     assert rc == gnlm.NLM_ERR_UNSUPPORTED
+
+
+def test_default_variants_without_autotune(L):
+    """Before any autotuning the forward uses the measured per-configuration default
+    (no GPU needed to read it)."""
+    fp16 = gnlm.NLM_FLAG_FP16_STORAGE
+    assert L.nlm_get_variant(3, 3, 1, 0) == 6   # 3D FP32 patch 3: z offsets in groups of three
+    assert L.nlm_get_variant(3, 5, 2, 0) == 5
+    assert L.nlm_get_variant(3, 3, 2, 0) == 0
+    assert L.nlm_get_variant(3, 3, 1, fp16) == 0
+    assert L.nlm_get_variant(3, 6, 8, 0) == 0   # large-patch kernel, 64-plane chunks
+    assert L.nlm_get_variant(2, 5, 2, 0) == 3   # 2D: y offsets in groups of three
+    assert L.nlm_get_variant(2, 10, 5, 0) == 4
+    for dims, flags in [(3, 0), (3, fp16), (2, 0)]:
+        assert L.nlm_variant_count(dims, flags) > L.nlm_get_variant(dims, 3, 1, flags)
