@@ -267,3 +267,31 @@ def test_3d_pipelined_host_path_matches_device_path(torch_cuda, gnlm_lib, shape,
     host = gnlm_lib.nlm3d_forward_host(pinned, sr, pr, h, fp16_storage=fp16,
                                        prepadded=u8_prepadded, shape=shape)
     assert np.array_equal(dev, host)
+
+
+def test_3d_volume_beyond_2_31_voxels(torch_cuda, gnlm_lib):
+    """40 x 6000 x 9000 = 2.16 G voxels (64-bit element indices in staging, kernel
+    output and the host-visible result): blocks at the corners and inside against
+    the FP64 direct form, each computed on a host crop that contains the block plus
+    its search+patch halo (crops that start at a volume border keep that border's
+    REFLECT_101; blocks stay H away from a crop's inner faces)."""
+    torch = torch_cuda
+    Z, Y, X = 40, 6000, 9000
+    assert Z * Y * X > 2 ** 31
+    g = torch.Generator(device="cuda").manual_seed(21)
+    v = torch.rand((Z, Y, X), device="cuda", generator=g)
+    # smooth structure plus noise: blend with a shifted copy so weights vary
+    v = (0.6 * v + 0.4 * torch.roll(v, shifts=(1, 2, 3), dims=(0, 1, 2))).contiguous()
+    out = gnlm_lib.nlm3d_forward(v, 3, 1, 0.05)
+    H = 4
+    blocks = [(0, 0, 0), (Z - 8, Y - 8, X - 8), (16, 3000, 4500), (0, Y - 8, 0), (32, 5100, 8200)]
+    for (z0, y0, x0) in blocks:
+        cz0, cy0, cx0 = max(0, z0 - 2 * H), max(0, y0 - 2 * H), max(0, x0 - 2 * H)
+        cz1, cy1, cx1 = min(Z, z0 + 8 + 2 * H), min(Y, y0 + 8 + 2 * H), min(X, x0 + 8 + 2 * H)
+        crop = v[cz0:cz1, cy0:cy1, cx0:cx1].cpu().numpy().astype(np.float64)
+        ref = O.nlm3d_region(crop, 3, 1, 0.05, (z0 - cz0, y0 - cy0, x0 - cx0), (8, 8, 8))
+        got = out[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8].cpu().numpy()
+        assert np.abs(got - ref).max() <= TOL_F32, (z0, y0, x0)
+    del v, out
+    torch.cuda.empty_cache()
+    assert gnlm_lib.device_status() == (0, 0)
