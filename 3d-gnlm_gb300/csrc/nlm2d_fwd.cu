@@ -85,6 +85,12 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
 
     const T* aptr = tile + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
+    if constexpr (kBoundsCheck) {  // offsets +-M around ROWS rows (groups reach the same rows)
+        const long long a0 = aptr - tile, reach = (long long)M * (C::BX + 1);
+        if (!range_ok(errword, a0 - reach, a0 + reach + (C::ROWS - 1) * C::BX,
+                      (long long)C::BX * C::BY))
+            aptr = tile + (C::H - N) * C::BX + M;  // warp 0, lane 0
+    }
     float2 areg[RP];
 #pragma unroll
     for (int rp = 0; rp < RP; ++rp)

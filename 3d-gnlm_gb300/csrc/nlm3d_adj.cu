@@ -122,9 +122,21 @@ __global__ void __launch_bounds__(32 * NW, 1)
     }
 
     // smem position of this thread's (row 0, plane 0) output voxel
-    const int sx = lane + C::HE + ral;
-    const int sy = warp * RY + C::HE;
+    int sx = lane + C::HE + ral;
+    int sy = warp * RY + C::HE;
     const int sz = C::HE;
+    if constexpr (kBoundsCheck) {  // v' window +-2N around the brick, offsets +-M; G/out' +-N
+        const long long reach = (long long)M * (C::PLANE + C::BX + 1), n = (long long)C::PLANE * C::BZ;
+        const long long v0 = (long long)(sz - 2 * N) * C::PLANE + (sy - 2 * N) * C::BX + sx;
+        const long long g0 = (long long)(sz - N) * C::PLANE + (sy - N) * C::BX + sx;
+        const bool ok =
+            range_ok(errword, v0 - reach, v0 + reach + (C::RT - 1) * C::BX + (C::PT - 1) * C::PLANE, n) &&
+            range_ok(errword, g0 - reach, g0 + reach + (C::RD - 1) * C::BX + (C::PD - 1) * C::PLANE, n);
+        if (!ok) {
+            sx = C::HE + ral;  // lane 0 of warp 0
+            sy = C::HE;
+        }
+    }
     // v' values of the difference window (same for every offset), as row pairs
     static_assert(C::RT % 2 == 0, "row pairs");
     constexpr int RTP = C::RT / 2;

@@ -225,7 +225,10 @@ void build_items(nlm_batch_plan* p, int v) {
     p->n_items = (int)p->items_host.size();
 }
 
-int set_error(int code, const char* msg) { return report_error(code, msg); }
+int set_error(int code, const char* msg) {
+    if (code == NLM_ERR_CUDA) cudaGetLastError();  // consume a non-sticky error
+    return report_error(code, msg);
+}
 
 // TMA boxes of tile shape v: the box must equal the tile the kernel expects for
 // the volume's search radius (columns 32 + 2 sr + 2 rounded to 16 bytes, TY + 2H

@@ -168,7 +168,38 @@ __global__ void __launch_bounds__(512, 1)
     // Stage A ownership: 16 lanes per halo row (conflict-free shared loads), lane
     // gi < NG owns columns 4*(G0+gi) .. +3 of the box.
     const int gi = tid & 15, ya = tid >> 4;
-    const bool hasA = gi < C::NG && ya < C::HY;
+    bool hasA = gi < C::NG && ya < C::HY;
+    // Stages B-D own fixed items too; a thread whose ranges leave their buffers
+    // (possible only through a defect, caught by NLM_BOUNDS_CHECK builds) skips its work.
+    bool okB = tid < C::NB, okC = tid < C::NC, okD = true;
+    if constexpr (kBoundsCheck) {
+        const long long szn = (long long)C::K * C::HY * C::PSZ, sxn = (long long)C::K * C::HY * C::PSX;
+        if (hasA) {
+            const int g = C::G0 + gi;
+            hasA = range_ok(a.errword, ya * C::BWR + 4 * gi, ya * C::BWR + 4 * gi + 3, C::REF_TX / 4) &&
+                   range_ok(a.errword, ya * C::BWC + 4 * (g - C::R),
+                            ya * C::BWC + 4 * (g + C::R) + 3, C::CAND_TX / 4) &&
+                   range_ok(a.errword, ya * C::PSZ + 4 * gi,
+                            ((C::K - 1) * C::HY + ya) * C::PSZ + 4 * gi + 3, szn);
+        }
+        if (okB) {
+            const int k = tid / C::HY, yh = tid - k * C::HY;
+            constexpr int NV = (C::MA + C::HX + 3) / 4;
+            okB = range_ok(a.errword, (k * C::HY + yh) * C::PSZ,
+                           (k * C::HY + yh) * C::PSZ + 4 * NV - 1, szn) &&
+                  range_ok(a.errword, (k * C::HY + yh) * C::PSX,
+                           (k * C::HY + yh) * C::PSX + C::CX - 1, sxn);
+        }
+        if (okC) {
+            const int k = tid >> 5, j = tid & 31;
+            okC = range_ok(a.errword, k * C::HY * C::PSX + j,
+                           k * C::HY * C::PSX + j + (C::HY - 1) * C::PSX, sxn);
+        }
+        const int y = tid >> 5, j = tid & 31;
+        okD = range_ok(a.errword, y * C::PSX + j, ((C::K - 1) * C::HY + y) * C::PSX + j, sxn) &&
+              range_ok(a.errword, (N + y) * C::BWC + 4 + N + j,
+                       (N + y) * C::BWC + 4 + N + j + C::K - 1, C::CAND_TX / 4);
+    }
     float Sz[C::K][4];
 
     int d = 0;  // output steps done
@@ -261,7 +292,7 @@ __global__ void __launch_bounds__(512, 1)
         if (tid == 0 && d + 1 < TD) issueD(lastD = d + 1);
 
         // B: x box sums along halo rows, two independent running sums of 16 outputs.
-        if (tid < C::NB) {
+        if (okB) {
             const int k = tid / C::HY, yh = tid - k * C::HY;
             const float* row = Szb + (k * C::HY + yh) * C::PSZ;
             constexpr int NV = (C::MA + C::HX + 3) / 4;
@@ -295,7 +326,7 @@ __global__ void __launch_bounds__(512, 1)
         __syncthreads();
         // C: y box sums down output columns, in place (row y of the column becomes D),
         // two independent running sums of 8 outputs.
-        if (tid < C::NC) {
+        if (okC) {
             const int k = tid >> 5, j = tid & 31;
             float* col = Sxb + k * C::HY * C::PSX + j;
             float u[C::HY];
@@ -322,11 +353,11 @@ __global__ void __launch_bounds__(512, 1)
         // D: weights and accumulation for voxel (X0 + j, Y0 + y, z).
         {
             const int db = d & 1;
-            const bool okD = mbar_wait_bounded(&barD[db], (d >> 1) & 1);
-            if (!okD) {
+            const bool okDw = mbar_wait_bounded(&barD[db], (d >> 1) & 1);
+            if (!okDw) {
                 raise_device_error(a.errword, DEVERR_TMA_TIMEOUT);
                 s_abort = 1;
-            } else {
+            } else if (okD) {
                 const int y = vy, j = vj;
                 const float* cpl =
                     reinterpret_cast<const float*>(dbuf(db)) + (N + y) * C::BWC + 4 + N + j;

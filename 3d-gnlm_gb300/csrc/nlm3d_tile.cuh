@@ -112,6 +112,13 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
 
     // Reference values: lane's column, rows warp*RY + H - N + rr, planes H - N + pl.
     const T* aptr = tile + (C::H - N) * C::PLANE + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
+    if constexpr (kBoundsCheck) {  // offsets +-M in every axis around ROWS x PLANES
+        const long long a0 = aptr - tile, reach = (long long)M * (C::PLANE + C::BX + 1);
+        if (!range_ok(errword, a0 - reach,
+                      a0 + reach + (C::ROWS - 1) * C::BX + (C::PLANES - 1) * C::PLANE,
+                      (long long)C::BX * C::BY * C::BZ))
+            aptr = tile + (C::H - N) * C::PLANE + (C::H - N) * C::BX + M;  // warp 0, lane 0
+    }
 
     float2 areg[AREG ? C::PLANES : 1][AREG ? RP : 1];
     if constexpr (AREG) {
@@ -289,6 +296,13 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
 
     const float* aptr =
         tile + (C::H - N) * C::PLANE + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
+    if constexpr (kBoundsCheck) {  // a group of GZ reads planes up to oz + PLANES + GZ - 2 <= M + PLANES - 1
+        const long long a0 = aptr - tile, reach = (long long)M * (C::PLANE + C::BX + 1);
+        if (!range_ok(errword, a0 - reach,
+                      a0 + reach + (C::ROWS - 1) * C::BX + (C::PLANES - 1) * C::PLANE,
+                      (long long)C::BX * C::BY * C::BZ))
+            aptr = tile + (C::H - N) * C::PLANE + (C::H - N) * C::BX + M;  // warp 0, lane 0
+    }
     float2 areg[C::PLANES][RP];
 #pragma unroll
     for (int pl = 0; pl < C::PLANES; ++pl)
@@ -503,8 +517,22 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
 
     // Row pair (r, r+1) of the tile, r = Y0 + j: in E at index j/2 if r is even, in O at
     // (j+1)/2 if odd.  The thread's rows start at j = warp*RY + M (+ oy for candidates).
-    const int col = lane + M + ral;
-    const int j0 = warp * RY + M;
+    int col = lane + M + ral;
+    int j0 = warp * RY + M;
+    if constexpr (kBoundsCheck) {  // row pairs of every oy in both copies, planes and columns +-M
+        long long lo = 1LL << 62, hi = -1;
+        for (int oy = -M; oy <= M; ++oy) {
+            const int jb = j0 + oy;
+            const long long pr0 = ((M + oy) & 1) ? (jb + 1) >> 1 : jb >> 1;
+            lo = min(lo, pr0 * C::BX + (long long)(C::H - N - M) * C::PLANEQ + col - M);
+            hi = max(hi, (pr0 + C::ROWS / 2 - 1) * C::BX +
+                             (long long)(C::H - N + M + C::PLANES - 1) * C::PLANEQ + col + M);
+        }
+        if (!range_ok(errword, lo, hi, (long long)C::BX * C::BYQ * C::BZ)) {
+            col = M;  // lane 0 of warp 0
+            j0 = M;
+        }
+    }
     const __half2* abase = (M & 1) ? O + ((j0 + 1) >> 1) * C::BX : E + (j0 >> 1) * C::BX;
     abase += (C::H - N) * C::PLANEQ + col;
     float2 areg[C::PLANES][RP];

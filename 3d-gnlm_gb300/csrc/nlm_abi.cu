@@ -34,6 +34,9 @@ int fail(int code, const char* fmt, ...) {
 }
 
 int cuda_fail(cudaError_t e, const char* what) {
+    // Consume a non-sticky error (e.g. a failed cudaMalloc) so that the next
+    // call's post-launch cudaGetLastError() does not report it again.
+    cudaGetLastError();
     if (e == cudaErrorNotSupported)
         return fail(NLM_ERR_UNSUPPORTED, "%s: combination not compiled in", what);
     return fail(NLM_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));

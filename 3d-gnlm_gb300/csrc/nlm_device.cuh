@@ -15,7 +15,33 @@ enum : unsigned int {
     DEVERR_TMA_TIMEOUT = 0x1u,     // a tile load did not complete within the wait limit
     DEVERR_QUEUE_TIMEOUT = 0x2u,   // a persistent-kernel queue wait gave up
     DEVERR_BAD_DESC = 0x4u,        // a work item failed its own bounds check
+    DEVERR_BOUNDS = 0x8u,          // NLM_BOUNDS_CHECK build: an index range left its buffer
 };
+
+// Builds compiled with -DNLM_BOUNDS_CHECK verify, once per tile or work item, that
+// the whole index range a thread is about to touch lies inside its buffer; a
+// violation sets DEVERR_BOUNDS and the caller redirects the thread to a range
+// known to be valid (no access leaves the buffer, no thread leaves a warp-wide
+// shuffle).  In normal builds the check compiles to nothing.
+#ifdef NLM_BOUNDS_CHECK
+constexpr bool kBoundsCheck = true;
+#else
+constexpr bool kBoundsCheck = false;
+#endif
+
+__device__ __forceinline__ void raise_device_error(unsigned int* word, unsigned int bits);
+
+// true when [lo, hi] lies inside [0, n) (always true unless NLM_BOUNDS_CHECK)
+__device__ __forceinline__ bool range_ok(unsigned int* errword, long long lo, long long hi,
+                                         long long n) {
+    if constexpr (kBoundsCheck) {
+        if (lo < 0 || hi >= n) {
+            raise_device_error(errword, DEVERR_BOUNDS);
+            return false;
+        }
+    }
+    return true;
+}
 
 // Upper bound on mbarrier.try_wait polls before a wait gives up.  Each poll may
 // suspend the thread for a hardware-defined interval, so this bounds the wait

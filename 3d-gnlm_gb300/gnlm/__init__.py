@@ -13,7 +13,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 PKG_DIR = os.path.dirname(_HERE)
 REPO_DIR = os.path.dirname(PKG_DIR)
 LIB_DIR = os.path.join(PKG_DIR, "lib")
-LIB_PATH = os.path.join(LIB_DIR, "libgnlm.so")
+# GNLM_LIB selects another build of the library, e.g. lib/libgnlm_checked.so (the
+# NLM_BOUNDS_CHECK build, whose kernels verify their index ranges at run time).
+LIB_PATH = os.environ.get("GNLM_LIB") or os.path.join(LIB_DIR, "libgnlm.so")
+CHECKED_LIB_PATH = os.path.join(LIB_DIR, "libgnlm_checked.so")
 LEGACY_LIB_PATH = os.path.join(LIB_DIR, "libgnlm_legacy.so")
 HEADER_DIR = os.path.join(REPO_DIR, "include")
 
