@@ -70,7 +70,10 @@ const char* nlm_last_error(void);
 
 /* Synchronises the current device, then reads and clears the device-side error
  * word that kernels set when a bounded wait gives up.  *flags receives the word
- * (0 = no error).  Returns NLM_OK, or NLM_ERR_DEVICE when the word was set. */
+ * (0 = no error; 0x1 a tile copy timed out, 0x2 a persistent-kernel queue wait gave
+ * up, 0x4 a batch work item failed its own check, 0x8 an index range left its
+ * buffer — reported only by the NLM_BOUNDS_CHECK build, libgnlm_checked.so).
+ * Returns NLM_OK, or NLM_ERR_DEVICE when the word was set. */
 int nlm_device_status(unsigned int* flags);
 
 /* Frees the library-cached workspaces and host-path buffers of every device. */
