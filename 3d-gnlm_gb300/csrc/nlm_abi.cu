@@ -159,8 +159,8 @@ int report_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
 // Variant used before any autotuning: the fastest measured on a GB300 for the
 // configuration family (3D FP32 patch 3: z offsets in groups of three, 4 x 8;
-// search 11 / patch 5: groups of three, 4 x 6; 2D FP32: y offsets in groups of
-// three, 8 warps for patch 11 and wider), else variant 0.
+// search 11 / patch 5: groups of three, 4 x 6; 2D FP32: two columns per lane, 8 rows
+// x 4 warps), else variant 0.
 int default_variant(int dims, int sr, int pr, bool fp16) {
     if (fp16) return 0;
     if (dims == 3) {
@@ -169,7 +169,7 @@ int default_variant(int dims, int sr, int pr, bool fp16) {
         if (pr == 2 && sr == 5) return 5;
         return 0;
     }
-    return pr >= 5 ? 4 : 3;
+    return 5;
 }
 
 int tuned_variant(int dims, int sr, int pr, bool fp16) {

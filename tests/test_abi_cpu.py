@@ -127,7 +127,8 @@ def test_default_variants_without_autotune(L):
     assert L.nlm_get_variant(3, 3, 2, 0) == 0
     assert L.nlm_get_variant(3, 3, 1, fp16) == 0
     assert L.nlm_get_variant(3, 6, 8, 0) == 0   # large-patch kernel, 64-plane chunks
-    assert L.nlm_get_variant(2, 5, 2, 0) == 3   # 2D: y offsets in groups of three
-    assert L.nlm_get_variant(2, 10, 5, 0) == 4
+    assert L.nlm_get_variant(2, 5, 2, 0) == 5   # 2D: two columns per lane
+    assert L.nlm_get_variant(2, 10, 5, 0) == 5
+    assert L.nlm_get_variant(2, 5, 2, fp16) == 0
     for dims, flags in [(3, 0), (3, fp16), (2, 0)]:
         assert L.nlm_variant_count(dims, flags) > L.nlm_get_variant(dims, 3, 1, flags)
