@@ -51,6 +51,24 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(dist, value, device):
+    """The largest `value` over all ranks (the slowest replica sets the job's time);
+    `value` itself without a process group.  `device` is where the reduction tensor
+    lives: "cuda" for NCCL, "cpu" for gloo."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, seconds_max):
+    """Whole-job throughput of `world` independent replicas, each processing
+    `units_per_rank` units: all units over the slowest replica's time."""
+    return world * units_per_rank / seconds_max
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
 
@@ -415,13 +433,9 @@ def run_gnlm(args):
     clocks = sampler.stop()
     if dist:
         dist.barrier()
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(dist, sum(step_ms), "cuda")
     ms_per_step = total_ms / args.steps
-    value = world * nvox / (ms_per_step * 1e-3) / 1e6
+    value = replica_throughput(nvox, world, ms_per_step * 1e-3) / 1e6
     out32 = out.clone()
 
     # FP16-storage form (same loop)
@@ -438,12 +452,8 @@ def run_gnlm(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         gnlm.nlm3d_forward_host(a_in, SR, PR, H, out=a_out)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_value = nvox / e2e_s / 1e6
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_value = world * nvox / float(t.item()) / 1e6
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.steps, "cuda")
+    e2e_value = replica_throughput(nvox, world, e2e_s) / 1e6
     assert np.array_equal(a_out, out32.cpu().numpy()), "host path disagrees with device path"
 
     if rank != 0:
