@@ -295,3 +295,34 @@ def test_3d_volume_beyond_2_31_voxels(torch_cuda, gnlm_lib):
     del v, out
     torch.cuda.empty_cache()
     assert gnlm_lib.device_status() == (0, 0)
+
+
+def test_3d_forward_captured_in_a_cuda_graph(torch_cuda, gnlm_lib):
+    """nlm3d_forward with a caller workspace is capturable: the staging pass and the
+    NLM kernel replay from a CUDA graph (tensor maps travel as kernel parameters) and
+    follow new input data written into the same buffer."""
+    torch = torch_cuda
+    shape = (24, 40, 70)
+    v1, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=5, sigma=0.05, seed=61)
+    v2, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=5, sigma=0.05, seed=62)
+    Z, Y, X = shape
+    x = torch.from_numpy(v1).cuda()
+    out = torch.empty_like(x)
+    ws = torch.empty(gnlm_lib.lib().nlm3d_workspace_bytes(X, Y, Z, 3, 1, 0), dtype=torch.uint8,
+                     device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        gnlm_lib.nlm3d_forward(x, 3, 1, 0.05, out=out, workspace=ws, stream=s)  # warm-up
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        gnlm_lib.nlm3d_forward(x, 3, 1, 0.05, out=out, workspace=ws,
+                               stream=torch.cuda.current_stream())
+    for v in (v1, v2):
+        x.copy_(torch.from_numpy(v))
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        direct = gnlm_lib.nlm3d_forward(torch.from_numpy(v).cuda(), 3, 1, 0.05).cpu().numpy()
+        assert np.array_equal(out.cpu().numpy(), direct)
+    assert gnlm_lib.device_status() == (0, 0)
