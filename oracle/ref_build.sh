@@ -59,6 +59,9 @@ build2d() {
 # only; its reads run past row ends, which the timing test covers with slack.
 build3d 7 3 120 128 16
 build3d 7 5 112 128 16
+# large-patch golden sizes (X a multiple of 33-NS): search 11 / patch 13, search 13 / patch 17
+build3d 11 13 120 128 8
+build3d 13 17 128 128 8
 # timing only (the 256^3 search-7 / patch-3 workload at the reference's own sizes)
 build3d 7 3 256 256 256 &
 build2d &

@@ -165,9 +165,14 @@ def inputs3d(SS, NS, X, Y, depth, kind, seed):
 def main(out_dir):
     os.makedirs(out_dir, exist_ok=True)
     drv = Driver()
-    for (SS, NS, X) in [(7, 3, 120), (7, 5, 112)]:
-        Y, depth = 128, 16
-        for kind, seed in [("zconst", 31), ("phantom", 32)]:
+    cases = [(7, 3, 120, 16, [("zconst", 31), ("phantom", 32)]),
+             (7, 5, 112, 16, [("zconst", 31), ("phantom", 32)]),
+             # large patches (the reference's NS 13..17 family), z-constant inputs
+             (11, 13, 120, 8, [("zconst", 34)]),
+             (13, 17, 128, 8, [("zconst", 35)])]
+    for (SS, NS, X, depth, kinds) in cases:
+        Y = 128
+        for kind, seed in kinds:
             padded = inputs3d(SS, NS, X, Y, depth, kind, seed)
             out = run3d(drv, SS, NS, X, Y, depth, padded)
             path = os.path.join(out_dir, f"ref3d_ss{SS}_ns{NS}_{kind}.npz")
