@@ -6,6 +6,7 @@
 // that reflects on every axis.  It reads the input once and writes the padded
 // copy once: algorithmic traffic = X*Y*Z*in_bytes + Xs*Yp*Zp*elem.
 #include <cuda_fp16.h>
+#include <stdint.h>
 
 #include "../../include/nlm.h"
 #include "nlm_device.cuh"
@@ -110,7 +111,43 @@ struct Vec16<__half> {
     }
 };
 
-template <typename Tin, typename Tout, bool PREPADDED>
+// NV consecutive input elements as floats in one vector load (the address is a
+// multiple of NV * sizeof(Tin), checked by the launcher).
+template <typename Tin, int NV>
+__device__ __forceinline__ void load_vec(const Tin* p, float* v) {
+    if constexpr (sizeof(Tin) * NV == 16) {
+        const uint4 u = *reinterpret_cast<const uint4*>(p);
+        const Tin* e = reinterpret_cast<const Tin*>(&u);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] = to_f32(e[i]);
+    } else if constexpr (sizeof(Tin) * NV == 32) {
+        const uint4 u0 = *reinterpret_cast<const uint4*>(p);
+        const uint4 u1 = *reinterpret_cast<const uint4*>(p + NV / 2);
+        const Tin* e0 = reinterpret_cast<const Tin*>(&u0);
+        const Tin* e1 = reinterpret_cast<const Tin*>(&u1);
+#pragma unroll
+        for (int i = 0; i < NV / 2; ++i) {
+            v[i] = to_f32(e0[i]);
+            v[NV / 2 + i] = to_f32(e1[i]);
+        }
+    } else if constexpr (sizeof(Tin) * NV == 8) {
+        const uint2 u = *reinterpret_cast<const uint2*>(p);
+        const Tin* e = reinterpret_cast<const Tin*>(&u);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] = to_f32(e[i]);
+    } else {
+        static_assert(sizeof(Tin) * NV == 4, "vector width");
+        const unsigned int u = *reinterpret_cast<const unsigned int*>(p);
+        const Tin* e = reinterpret_cast<const Tin*>(&u);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] = to_f32(e[i]);
+    }
+}
+
+// VEC: every source row starts on a multiple of V::N elements and the halo H is one
+// too (not prepadded), so the chunks that lie inside the source row are one vector
+// load each; the 2H border columns and the stride padding take the scalar path.
+template <typename Tin, typename Tout, bool PREPADDED, bool VEC>
 __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
                                                     int Z, int H, int Hz, int Xp, int Yp,
                                                     long long row0, long long row1, int Xs,
@@ -129,23 +166,45 @@ __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, 
         const int sy = reflect101(py - H, Y);
         srow = in + ((size_t)sz * Y + sy) * X;
     }
-    for (int c = lane; c * V::N < Xs; c += 32) {
-        float v[V::N];
+    const int sh = PREPADDED ? 0 : H;      // source column = padded column - sh
+    const int slen = PREPADDED ? Xp : X;   // source row length
+    auto chunk = [&](int c, float* v) {
+        const int px0 = c * V::N;
+        if (VEC && px0 >= sh && px0 - sh + V::N <= slen) {
+            load_vec<Tin, V::N>(srow + (px0 - sh), v);
+        } else {
 #pragma unroll
-        for (int i = 0; i < V::N; ++i) {
-            const int px = c * V::N + i;
-            float x = 0.f;
-            if (px < Xp) {
-                int sx = px;
-                if (!PREPADDED) {
-                    sx = px - H;
-                    if (sx < 0 || sx >= X) sx = reflect101(sx, X);
+            for (int i = 0; i < V::N; ++i) {
+                const int px = px0 + i;
+                float x = 0.f;
+                if (px < Xp) {
+                    int sx = px;
+                    if (!PREPADDED) {
+                        sx = px - H;
+                        if (sx < 0 || sx >= X) sx = reflect101(sx, X);
+                    }
+                    x = to_f32(srow[sx]);
                 }
-                x = to_f32(srow[sx]) * scale;
+                v[i] = x;
             }
-            v[i] = x;
         }
-        drow[c] = V::pack(v);
+#pragma unroll
+        for (int i = 0; i < V::N; ++i) v[i] *= scale;
+    };
+    // two chunks per iteration, both loads issued before either store
+    const int nchunk = Xs / V::N;
+    int c = lane;
+    for (; c + 32 < nchunk; c += 64) {
+        float v0[V::N], v1[V::N];
+        chunk(c, v0);
+        chunk(c + 32, v1);
+        drow[c] = V::pack(v0);
+        drow[c + 32] = V::pack(v1);
+    }
+    if (c < nchunk) {
+        float v0[V::N];
+        chunk(c, v0);
+        drow[c] = V::pack(v0);
     }
 }
 
@@ -154,14 +213,20 @@ static cudaError_t stage_typed(const void* in, bool prepadded, float scale, cons
                                void* dst, cudaStream_t stream, int pz0, int pz1) {
     const long long row0 = (long long)st.Yp * pz0, row1 = (long long)st.Yp * pz1;
     const unsigned blocks = (unsigned)((row1 - row0 + 7) / 8);
-    if (prepadded)
-        stage_kernel<Tin, Tout, true><<<blocks, 256, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, row0, row1, st.Xs, scale,
-            (Tout*)dst);
-    else
-        stage_kernel<Tin, Tout, false><<<blocks, 256, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, row0, row1, st.Xs, scale,
-            (Tout*)dst);
+    constexpr int NV = Vec16<Tout>::N;
+    const size_t vbytes = sizeof(Tin) * NV;
+    const bool vec = reinterpret_cast<uintptr_t>(in) % vbytes == 0 &&
+                     (prepadded ? st.Xp % NV == 0 : (st.X % NV == 0 && st.H % NV == 0));
+#define GNLM_STAGE_LAUNCH(P, VEC)                                                              \
+    stage_kernel<Tin, Tout, P, VEC><<<blocks, 256, 0, stream>>>(                                \
+        (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, row0, row1, st.Xs, scale, \
+        (Tout*)dst)
+    if (prepadded) {
+        if (vec) GNLM_STAGE_LAUNCH(true, true); else GNLM_STAGE_LAUNCH(true, false);
+    } else {
+        if (vec) GNLM_STAGE_LAUNCH(false, true); else GNLM_STAGE_LAUNCH(false, false);
+    }
+#undef GNLM_STAGE_LAUNCH
     return cudaGetLastError();
 }
 
