@@ -326,3 +326,44 @@ def test_3d_forward_captured_in_a_cuda_graph(torch_cuda, gnlm_lib):
         direct = gnlm_lib.nlm3d_forward(torch.from_numpy(v).cuda(), 3, 1, 0.05).cpu().numpy()
         assert np.array_equal(out.cpu().numpy(), direct)
     assert gnlm_lib.device_status() == (0, 0)
+
+
+def test_concurrent_calls_from_host_threads(torch_cuda, gnlm_lib):
+    """Four host threads, each on its own stream (its own cached workspace), call the
+    3D forward (small- and large-patch kernels) and the 2D forward concurrently; every
+    result equals the same call made alone."""
+    import threading
+    torch = torch_cuda
+    v, _ = phantom.ellipsoid_phantom((20, 33, 47), n_ellipsoids=5, sigma=0.05, seed=71)
+    im, _ = phantom.disc_rect_phantom((90, 130), n_shapes=6, sigma=0.08, seed=72)
+    jobs = [(3, 3, 1, 0.05), (3, 5, 6, 0.05), (3, 2, 1, 0.07), (2, 5, 2, 0.08)]
+
+    def run(dims, sr, pr, h, stream=None):
+        if dims == 3:
+            return gnlm_lib.nlm3d_forward(torch.from_numpy(v).cuda(), sr, pr, h, stream=stream)
+        return gnlm_lib.nlm2d_forward(torch.from_numpy(im).cuda(), sr, pr, h, stream=stream)
+
+    expected = [run(*j).cpu().numpy() for j in jobs]
+    results = [None] * len(jobs)
+    errors = []
+
+    def worker(i):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                outs = [run(*jobs[i], stream=s) for _ in range(5)]
+            s.synchronize()
+            results[i] = [o.cpu().numpy() for o in outs]
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(len(jobs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for i, outs in enumerate(results):
+        for o in outs:
+            assert np.array_equal(o, expected[i]), jobs[i]
+    assert gnlm_lib.device_status() == (0, 0)
