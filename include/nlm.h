@@ -62,10 +62,12 @@ typedef enum nlm_dtype {
                                       distances, Kahan-compensated weight sums */
 #define NLM_FLAG_PREPADDED 0x2u    /* input is already padded by sr+pr per side */
 
-/* Library identification, e.g. "gnlm 0.1 sm_103a". */
+/* Library identification, e.g. "gnlm 0.1 sm_103a" (no counterpart in the reference). */
 const char* nlm_version(void);
 
-/* Message of the calling thread's last failing call ("" if none). */
+/* Message of the calling thread's last failing call ("" if none).  With the status
+ * codes, replaces the reference's CUDA_CHECK printing to stderr
+ * (3DNLM/cuda_utility.h:9-16), which its NL_Means ignores. */
 const char* nlm_last_error(void);
 
 /* Synchronises the current device, then reads and clears the device-side error
@@ -76,7 +78,9 @@ const char* nlm_last_error(void);
  * Returns NLM_OK, or NLM_ERR_DEVICE when the word was set. */
 int nlm_device_status(unsigned int* flags);
 
-/* Frees the library-cached workspaces and host-path buffers of every device. */
+/* Frees the library-cached workspaces and host-path buffers of every device (the
+ * reference allocates and frees its buffers inside every NL_Means call,
+ * 3DNLM/main.cu:7616-7618,7672-7674). */
 int nlm_release_cached(void);
 
 /* ---------------------------------------------------------------- 3D ------ */
