@@ -80,7 +80,7 @@ int nlm_device_status(unsigned int* flags);
 
 /* Frees the library-cached workspaces and host-path buffers of every device (the
  * reference allocates and frees its buffers inside every NL_Means call,
- * 3DNLM/main.cu:7616-7618,7672-7674). */
+ * 3DNLM/main.cu:7616-7618,7674-7676). */
 int nlm_release_cached(void);
 
 /* ---------------------------------------------------------------- 3D ------ */
