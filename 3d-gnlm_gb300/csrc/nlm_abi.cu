@@ -531,7 +531,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const int variant = tuned_variant(3, sr, pr, fp16);
     const int RZ = nlm3d_fwd_tile_z(sr, pr, fp16, variant);
     if (RZ <= 0) return 1;
-    const int CZ = std::max(1, (Z / 8 + RZ - 1) / RZ) * RZ;
+    const int CZ = std::max(1, (Z / 16 + RZ - 1) / RZ) * RZ;
     const int nch = (Z + CZ - 1) / CZ;
     if (nch < 2) return 1;
     cudaError_t e = cudaSuccess;
