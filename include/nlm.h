@@ -24,7 +24,9 @@
  *   - Scratch: each forward call needs a workspace.  Pass d_ws/ws_bytes (size
  *     from the *_workspace_bytes query), or d_ws = NULL to use a buffer the
  *     library caches per (device, stream) and grows with cudaMalloc; the cache
- *     grows only outside stream capture, so warm it before capturing.
+ *     grows only outside stream capture, so warm it before capturing.  Each
+ *     distinct stream keeps its own buffer until nlm_release_cached(): callers
+ *     that create a new stream per call should pass their own workspace.
  *   - Thread safety: calls are thread-safe; calls on different streams with the
  *     library cache use different buffers.
  */
