@@ -250,10 +250,16 @@ int nlm_release_cached(void) {
     std::lock_guard<std::mutex> lk(g_mutex);
     int prev = 0;
     cudaGetDevice(&prev);
+    // A device-wide synchronise rather than one per cached stream: the caller may
+    // already have destroyed a stream whose workspace is cached.
+    int synced = -1;
     for (auto& kv : g_ws) {
         if (kv.second.first) {
-            cudaSetDevice(kv.first.first);
-            cudaStreamSynchronize(kv.first.second);
+            if (kv.first.first != synced) {
+                cudaSetDevice(kv.first.first);
+                cudaDeviceSynchronize();
+                synced = kv.first.first;
+            }
             cudaFree(kv.second.first);
         }
     }
