@@ -189,9 +189,11 @@ bool nlm3d_fwd_large_patch(int sr, int pr, bool fp16) {
     return !fp16 && !small_case(sr, pr) && nlm3d_lp_supported(sr, pr);
 }
 
+// Two (Z, num) accumulator buffers: the large-patch launcher may split each tile's
+// passes into two halves (nlm3d_lp_split).
 size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16) {
     if (!nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
-    return align_up((size_t)X * Y * Z * sizeof(float2), kAlign);
+    return align_up(2 * (size_t)X * Y * Z * sizeof(float2), kAlign);
 }
 
 int nlm3d_fwd_tile_z(int sr, int pr, bool fp16, int v) {

@@ -1,8 +1,48 @@
 // Large-patch 3D forward: instances and launch (kernel in nlm3d_lp.cuh).
+#include <algorithm>
+
 #include "nlm3d_lp.cuh"
 #include "nlm_internal.h"
 
 namespace gnlm {
+
+// out = (num_0 + num_1) / (Z_0 + Z_1) over the voxels [v0, v0 + n) of two
+// accumulator buffers (the two halves of the passes), always added in that order.
+__global__ void __launch_bounds__(256) lp_combine_kernel(const float2* __restrict__ acc,
+                                                         size_t stride, size_t v0, size_t n,
+                                                         float inv_scale, float* __restrict__ out,
+                                                         float* __restrict__ zsum) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t v = v0 + i;
+        const float2 h0 = acc[v], h1 = acc[stride + v];
+        const float zt = h0.x + h1.x, nt = h0.y + h1.y;
+        out[v] = nt / zt * inv_scale;
+        if (zsum) zsum[v] = zt;
+    }
+}
+
+static int sm_count() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return 1;
+    return sms;
+}
+
+// Pass split of a whole volume (one CTA per SM): two half-pass CTAs per tile when
+// that fills the last wave better, estimated as ceil(2n / SMs) / 2 against
+// ceil(n / SMs) waves of full-pass CTAs.  Depends only on the volume, the chunk
+// depth and the device, so every launch over one volume (whole or by chunk
+// ranges) makes the same choice and the sums are the same bits.
+int nlm3d_lp_split(int X, int Y, int Z, int tz) {
+    if (tz <= 0) return 1;
+    const long long n = (long long)((X + 31) / 32) * ((Y + 15) / 16) * ((Z + tz - 1) / tz);
+    const long long sms = sm_count();
+    const double one = (double)((n + sms - 1) / sms);
+    const double two = (double)((2 * n + sms - 1) / sms) / 2.0;
+    return two < 0.97 * one ? 2 : 1;
+}
 
 template <int M, int N>
 static cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,
@@ -23,19 +63,31 @@ static cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     if (e != cudaSuccess) return e;
     if (zc1 < 0) zc1 = (st.Z + tz - 1) / tz;
     if (zc1 <= zc0) return cudaSuccess;
+    const int nsplit = nlm3d_lp_split(st.X, st.Y, st.Z, tz);
     LpArgs a;
     a.X = st.X;
     a.Y = st.Y;
     a.Z = st.Z;
     a.TZ = tz;
     a.zc0 = zc0;
+    a.nzc = zc1 - zc0;
+    a.nsplit = nsplit;
+    a.part_stride = (size_t)st.X * st.Y * st.Z;
     a.inv_scale = inv_scale;
     a.acc = acc;
     a.out = out;
     a.zsum = zsum;
     a.errword = errword;
-    dim3 grid((st.X + C::CX - 1) / C::CX, (st.Y + C::CY - 1) / C::CY, zc1 - zc0);
+    dim3 grid((st.X + C::CX - 1) / C::CX, (st.Y + C::CY - 1) / C::CY, (zc1 - zc0) * nsplit);
     kern<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(mapR, mapC, a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || nsplit == 1) return e;
+    const size_t plane = (size_t)st.X * st.Y;
+    const size_t v0 = (size_t)zc0 * tz * plane;
+    const size_t v1 = (size_t)std::min(zc1 * tz, st.Z) * plane;
+    const size_t blocks = std::min<size_t>((v1 - v0 + 255) / 256, (size_t)sm_count() * 8);
+    lp_combine_kernel<<<(unsigned)blocks, 256, 0, stream>>>(acc, a.part_stride, v0, v1 - v0,
+                                                            inv_scale, out, zsum);
     return cudaGetLastError();
 }
 

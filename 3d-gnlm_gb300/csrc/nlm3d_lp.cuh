@@ -25,6 +25,10 @@
 //      pair in the accumulator buffer (L2-resident: a chunk's pairs are re-read
 //      once per pass, in pass order, so the sums are deterministic).  The last
 //      pass writes out = num / Z (3DNLM/main.cu:125).
+// With one CTA per SM, a grid of a few waves can leave most of the last wave
+// idle; the launcher may then split each tile's passes into two halves run by
+// two CTAs with separate accumulator buffers, and a combine kernel adds the two
+// halves (always in the same order) and writes num / Z.
 #pragma once
 
 #include "nlm3d_tile.cuh"
@@ -83,8 +87,11 @@ struct LpArgs {
     int X, Y, Z;
     int TZ;           // planes per chunk
     int zc0;          // first chunk of this launch
+    int nzc;          // chunks in this launch (grid z = nzc * nsplit)
+    int nsplit;       // 1: a CTA makes every pass; 2: each half of the passes
+    size_t part_stride;  // float2 pairs per accumulator buffer (X * Y * Z)
     float inv_scale;
-    float2* acc;      // (Z, num) pairs, [Z][Y][X]
+    float2* acc;      // (Z, num) pairs, [nsplit][Z][Y][X]
     float* out;
     float* zsum;
     unsigned int* errword;
@@ -104,14 +111,18 @@ __global__ void __launch_bounds__(512, 1)
 
     const int tid = threadIdx.x;
     const int X0 = blockIdx.x * C::CX, Y0 = blockIdx.y * C::CY;
-    const int Z0 = (blockIdx.z + a.zc0) * a.TZ;
+    const int chunk = blockIdx.z % a.nzc, part = blockIdx.z / a.nzc;
+    const int Z0 = (chunk + a.zc0) * a.TZ;
     const int TZc = min(a.TZ, a.Z - Z0);
     if (TZc <= 0) return;  // uniform over the CTA
+    // This CTA's passes [pb, pb + P) of the (2sr+1)^2, and its accumulator buffer.
+    const int pb = part * (C::K * C::K) / a.nsplit;
+    const int P = (part + 1) * (C::K * C::K) / a.nsplit - pb;
+    float2* const acc = a.acc + part * a.part_stride;
     // A pass is N warm-up steps, each adding two planes of the first window
     // (padded planes Z0+M .. Z0+M+2N-1), then TZc output steps: output plane
     // Z0+q adds padded plane Z0+M+2N+q and, for q >= 1, drops Z0+M+q-1.
     const int SPP = N + TZc;
-    const int P = C::K * C::K;  // passes
     const int T = P * SPP;      // steps
     const int TD = P * TZc;     // output steps
 
@@ -121,7 +132,7 @@ __global__ void __launch_bounds__(512, 1)
     // Thread 0: loads of step t's planes into A buffer t&1 (slot 0: the entering
     // plane, slot 1: the second warm-up plane or the leaving plane).
     auto issueA = [&](int t) {
-        const int b = t & 1, pass = t / SPP, s = t - pass * SPP;
+        const int b = t & 1, lp = t / SPP, s = t - lp * SPP, pass = pb + lp;
         const int oz = pass / C::K - M, oy = pass % C::K - M;
         int p0, p1 = -1;
         if (s < N) {
@@ -146,7 +157,7 @@ __global__ void __launch_bounds__(512, 1)
     };
     // Thread 0: the candidate plane of output step d (stage D's centre values).
     auto issueD = [&](int d) {
-        const int b = d & 1, pass = d / TZc, q = d - pass * TZc;
+        const int b = d & 1, lp = d / TZc, q = d - lp * TZc, pass = pb + lp;
         const int oz = pass / C::K - M, oy = pass % C::K - M;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&barD[b], C::CAND_TX);
@@ -220,7 +231,7 @@ __global__ void __launch_bounds__(512, 1)
         const bool vin = out_step && vx < a.X && vyy < a.Y;
         const size_t vo = ((size_t)vz * a.Y + vyy) * a.X + vx;
         float2 prev = make_float2(0.f, 0.f);
-        if (vin && pass > 0) prev = a.acc[vo];
+        if (vin && pass > 0) prev = acc[vo];
         const int b = t & 1;
         const bool okA = mbar_wait_bounded(&barA[b], (t >> 1) & 1);
         if (!okA) {
@@ -371,11 +382,11 @@ __global__ void __launch_bounds__(512, 1)
                 if (vin) {
                     const float zt = prev.x + (zl[0] + zl[1]);
                     const float nt = prev.y + (nl[0] + nl[1]);
-                    if (pass == P - 1) {
+                    if (pass == P - 1 && a.nsplit == 1) {
                         a.out[vo] = nt / zt * a.inv_scale;
                         if (a.zsum) a.zsum[vo] = zt;
                     } else {
-                        a.acc[vo] = make_float2(zt, nt);
+                        acc[vo] = make_float2(zt, nt);
                     }
                 }
             }

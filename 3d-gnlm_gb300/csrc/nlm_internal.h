@@ -54,7 +54,7 @@ cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float sca
 // [zt0, zt1): range of z tiles to compute (zt1 < 0: through the last); a z tile
 // is nlm3d_fwd_tile_z(sr, pr, fp16, variant) output planes.
 // Large-patch configurations (nlm3d_fwd_large_patch) keep per-voxel (Z, num)
-// accumulator pairs in the workspace right after the staged volume:
+// accumulator pairs (two buffers) in the workspace right after the staged volume:
 // nlm3d_fwd_extra_bytes() more bytes at staged + st.bytes().
 cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
                              int variant, float inv_scale, float* out, float* zsum,
@@ -69,6 +69,7 @@ size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16);
 // Large-patch kernel (nlm3d_lp.cu): chunk depth per variant, compiled pairs, launch.
 int nlm3d_lp_tile_z(int variant);
 bool nlm3d_lp_supported(int sr, int pr);
+int nlm3d_lp_split(int X, int Y, int Z, int tz);
 cudaError_t launch_nlm3d_lp(const Staging& st, const void* staged, int sr, int pr, int variant,
                             float inv_scale, float* out, float* zsum, float2* acc,
                             unsigned int* errword, cudaStream_t stream, int zc0, int zc1);

@@ -128,3 +128,19 @@ def test_large_patch_sweep_size_spot_checks(torch_cuda, gnlm_lib):
         o = O.nlm3d_region(v, 6, 8, 0.05, (z0, y0, x0), (4, 4, 4))
         assert np.abs(g[z0:z0 + 4, y0:y0 + 4, x0:x0 + 4] - o).max() <= TOL, (z0, y0, x0)
     assert gnlm_lib.device_status() == (0, 0)
+
+
+def test_large_patch_split_and_whole_passes(torch_cuda, gnlm_lib):
+    """One CTA per SM: a grid that leaves the last wave mostly idle splits each tile's
+    passes into two halves with separate accumulators, added by a combine kernel;
+    a grid of whole waves does not.  On a 152-SM GB300, 250 x 300 x 4 is 8 x 19 tiles
+    = exactly one wave (no split) and 250 x 144 x 4 is 8 x 9 tiles, under half a wave
+    (split).  Both match the FP64 oracle, and repeated calls give the same bits."""
+    for shape in [(4, 300, 250), (4, 144, 250)]:
+        v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=8, sigma=0.05, seed=shape[1],
+                                         radii=(3.0, 20.0))
+        g = _gpu3d(torch_cuda, gnlm_lib, v, 1, 3, 0.05)
+        o = O.nlm3d(v, 1, 3, 0.05, dtype=np.float64)
+        assert np.abs(g - o).max() <= TOL, shape
+        assert np.array_equal(g, _gpu3d(torch_cuda, gnlm_lib, v, 1, 3, 0.05))
+    assert gnlm_lib.device_status() == (0, 0)
