@@ -91,7 +91,7 @@ int nlm_release_cached(void);
  * Compiled (sr, pr): sr 1..5 with pr 1, sr 3 and 5 with pr 2 (register-brick
  * kernel, FP32 or FP16 storage), and sr 1..6 with pr 1..8 otherwise
  * (large-patch kernel, FP32 only: the reference's NS 7..17 configurations);
- * for the latter the scratch also holds one (Z, num) float pair per voxel. */
+ * for the latter the scratch also holds two (Z, num) float pairs per voxel. */
 size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags);
 
 /*
