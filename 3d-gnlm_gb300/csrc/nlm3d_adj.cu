@@ -14,10 +14,14 @@
 // each output voxel is written by exactly one thread (a gather, no atomics), and the
 // h reduction is two fixed-order passes, so results are bitwise reproducible.
 //
-// Kernels: adj_aux_kernel (G and out' padded like the staged volume),
-// nlm3d_adj_kernel (gpad' over the padded domain + per-CTA h partial sums),
+// Kernels: adj_aux_kernel ((G, out') pairs padded like the staged volume),
+// nlm3d_adj_kernel (gpad' over the padded domain + per-CTA h partial sums; the
+// tiles of a last, partial wave are split by offset runs over several CTAs whose
+// partial gpad' adj_tail_combine_kernel adds in part order),
 // adj_fold_kernel (REFLECT_101 fold, times s), adj_hgrad_kernel (ordered sum).
 #include <cuda_fp16.h>
+
+#include <algorithm>
 
 #include "nlm_device.cuh"
 #include "nlm_internal.h"
@@ -36,70 +40,122 @@ struct Adj3d {
     static constexpr int BY = TY + 2 * HE;
     static constexpr int BZ = RZ + 2 * HE;
     static constexpr int PLANE = BX * BY;
-    static constexpr int FIELD_BYTES = BX * BY * BZ * 4;
-    // each field starts on a 128-byte boundary: TMA tensor-copy destinations must
+    static constexpr int FIELD_BYTES = BX * BY * BZ * 4;     // v' tile
+    static constexpr int GO_BYTES = 2 * FIELD_BYTES;         // (G, out') pair tile
+    // each tile starts on a 128-byte boundary: TMA tensor-copy destinations must
     static constexpr int FIELD_STRIDE = adj_round(FIELD_BYTES, 128);
-    static constexpr int BAR_OFF = 3 * FIELD_STRIDE;          // mbarrier
+    static constexpr int GO_STRIDE = adj_round(GO_BYTES, 128);
+    static constexpr int BAR_OFF = FIELD_STRIDE + GO_STRIDE;  // mbarrier
     static constexpr int RED_OFF = BAR_OFF + 128;             // per-warp h partials
     static constexpr int SMEM_BYTES = RED_OFF + 32 * 8;
     static_assert(FIELD_STRIDE % 128 == 0 && BAR_OFF % 128 == 0, "TMA destination alignment");
     static constexpr int K = 2 * N + 1;
+    static constexpr int TILE_VOX = RZ * TY * 32;           // floats of a partial brick tile
     static constexpr int RT = RY + 4 * N, PT = RZ + 4 * N;  // difference window
     static constexpr int RD = RY + 2 * N, PD = RZ + 2 * N;  // distance window
-    static_assert(BX <= 256 && BY <= 256 && BZ <= 256, "TMA box dimension > 256");
+    static_assert(2 * BX <= 256 && BY <= 256 && BZ <= 256, "TMA box dimension > 256");
     static_assert(SMEM_BYTES <= 227 * 1024, "adjoint tile exceeds shared memory");
+    static_assert(RY % 2 == 0 && RZ % 2 == 0, "outputs are processed in pairs");
 };
 
-// G = g / (s Z) and out' = s out, padded like the staged volume (zero outside).
+// (G, out') = (g / (s Z), s out) pairs, padded like the staged volume (zero outside).
 __global__ void __launch_bounds__(256) adj_aux_kernel(const float* __restrict__ g,
                                                       const float* __restrict__ out,
                                                       const float* __restrict__ zsum, int X,
                                                       int Y, int Z, int H, int Xs, int Yp,
-                                                      float s, float* __restrict__ G,
-                                                      float* __restrict__ O) {
+                                                      float s, float2* __restrict__ GO) {
     const int py = blockIdx.x, pz = blockIdx.y;
     const int y = py - H, z = pz - H;
     const bool inside_yz = y >= 0 && y < Y && z >= 0 && z < Z;
-    float* grow = G + ((size_t)pz * Yp + py) * Xs;
-    float* orow = O + ((size_t)pz * Yp + py) * Xs;
+    float2* row = GO + ((size_t)pz * Yp + py) * Xs;
     for (int px = threadIdx.x; px < Xs; px += blockDim.x) {
         const int x = px - H;
-        float gv = 0.f, ov = 0.f;
+        float2 go = make_float2(0.f, 0.f);
         if (inside_yz && x >= 0 && x < X) {
             const size_t i = ((size_t)z * Y + y) * X + x;
-            gv = g[i] / (s * zsum[i]);
-            ov = s * out[i];
+            go = make_float2(g[i] / (s * zsum[i]), s * out[i]);
         }
-        grow[px] = gv;
-        orow[px] = ov;
+        row[px] = go;
     }
 }
+
+// out[i] = in[i] + ... + in[i + K - 1] for i < NO (NO even); each pair of outputs
+// shares its K - 1 middle terms.
+template <int K, int NO>
+__device__ __forceinline__ void box_pairs(const float (&in)[NO + K - 1], float (&out)[NO]) {
+    static_assert(NO % 2 == 0, "pairs");
+#pragma unroll
+    for (int i = 0; i < NO; i += 2) {
+        float u = in[i + 1];
+#pragma unroll
+        for (int k = 2; k < K; ++k) u += in[i + k];
+        out[i] = in[i] + u;
+        out[i + 1] = u + in[i + K];
+    }
+}
+
+// x box sum across lanes of a pair of values: the shuffles per value, the adds packed.
+template <int N>
+__device__ __forceinline__ float2 xbox_pair(float2 y) {
+    if constexpr (N == 1) {
+        const float2 dn = make_float2(__shfl_down_sync(0xffffffffu, y.x, 1),
+                                      __shfl_down_sync(0xffffffffu, y.y, 1));
+        const float2 up = make_float2(__shfl_up_sync(0xffffffffu, y.x, 1),
+                                      __shfl_up_sync(0xffffffffu, y.y, 1));
+        return __fadd2_rn(y, __fadd2_rn(dn, up));
+    } else {
+        return make_float2(xbox_lanes<N>(y.x), xbox_lanes<N>(y.y));
+    }
+}
+
+// Work split of one launch (1D grid): CTAs [0, full) own tiles [0, full) whole;
+// each of the ntail tiles after them is split into S parts, CTA full + t*S + p
+// making part p of the (2M+1)^2 (oz, oy) offset runs of tile full + t and writing
+// its partial gpad' brick to side[(p * ntail + t) * tile_vox ...].
+struct AdjTail {
+    int nx, ny;   // tiles along x and y
+    int full;     // tiles made whole by one CTA
+    int S;        // parts per tail tile
+    int ntail;    // tail tiles
+    float* side;  // S * ntail partial bricks (tile_vox floats each)
+};
 
 template <int M, int N, int RY, int RZ, int NW>
 __global__ void __launch_bounds__(32 * NW, 1)
     nlm3d_adj_kernel(const __grid_constant__ CUtensorMap vmap,
-                     const __grid_constant__ CUtensorMap gmap,
-                     const __grid_constant__ CUtensorMap omap, int X, int Y, int Z, int Xs, int Yp,
-                     float* __restrict__ gpad, double* __restrict__ hpart,
+                     const __grid_constant__ CUtensorMap gomap, int X, int Y, int Z, int Xs, int Yp,
+                     float* __restrict__ gpad, double* __restrict__ hpart, const AdjTail tl,
                      unsigned int* errword) {
     using C = Adj3d<M, N, RY, RZ, NW>;
     constexpr float kLn2 = 0.69314718055994531f;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* vt = reinterpret_cast<float*>(smem_raw);
-    float* gt = reinterpret_cast<float*>(smem_raw + C::FIELD_STRIDE);
-    float* ot = reinterpret_cast<float*>(smem_raw + 2 * C::FIELD_STRIDE);
+    float2* got = reinterpret_cast<float2*>(smem_raw + C::FIELD_STRIDE);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF);
     double* red = reinterpret_cast<double*>(smem_raw + C::RED_OFF);
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int Xp = X + 2 * C::H, Ypd = Y + 2 * C::H, Zp = Z + 2 * C::H;
+    // Tile and offset runs of this CTA (uniform over the CTA).
+    constexpr int RUNS = (2 * M + 1) * (2 * M + 1);
+    int tile, part = 0, nparts = 1;
+    if ((int)blockIdx.x < tl.full) {
+        tile = blockIdx.x;
+    } else {
+        const int j = blockIdx.x - tl.full;
+        tile = tl.full + j / tl.S;
+        part = j - (j / tl.S) * tl.S;
+        nparts = tl.S;
+    }
+    const int run0 = part * RUNS / nparts, run1 = (part + 1) * RUNS / nparts;
+    const int bx = tile % tl.nx, by = (tile / tl.nx) % tl.ny, bz = tile / (tl.nx * tl.ny);
     // Output positions are padded-domain voxels, staged coordinates [0, Xp) etc.
     // smem column 0 starts HE voxels before lane 0's voxel (staged x = bx*XO - 2N)
-    const int base_x = blockIdx.x * C::XO - 2 * N - C::HE;
+    const int base_x = bx * C::XO - 2 * N - C::HE;
     const int org_x = base_x & ~3;                  // 16-byte aligned TMA start (may be < 0)
     const int ral = base_x - org_x;
-    const int Y0 = blockIdx.y * C::TY, Z0 = blockIdx.z * RZ;
+    const int Y0 = by * C::TY, Z0 = bz * RZ;
     const int org_y = Y0 - C::HE, org_z = Z0 - C::HE;
 
     if (threadIdx.x == 0) {
@@ -108,10 +164,9 @@ __global__ void __launch_bounds__(32 * NW, 1)
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(bar, 3 * C::FIELD_BYTES);
+        mbar_arrive_expect_tx(bar, C::FIELD_BYTES + C::GO_BYTES);
         tma_load_3d(vt, &vmap, org_x, org_y, org_z, bar);
-        tma_load_3d(gt, &gmap, org_x, org_y, org_z, bar);
-        tma_load_3d(ot, &omap, org_x, org_y, org_z, bar);
+        tma_load_3d(got, &gomap, 2 * org_x, org_y, org_z, bar);
     }
     if (!mbar_wait_bounded(bar, 0)) {
         if (threadIdx.x == 0) {
@@ -139,10 +194,10 @@ __global__ void __launch_bounds__(32 * NW, 1)
     }
     // v' values of the difference window (same for every offset), as row pairs
     static_assert(C::RT % 2 == 0, "row pairs");
-    constexpr int RTP = C::RT / 2;
+    constexpr int K = C::K, RTP = C::RT / 2, RD = C::RD, PD = C::PD;
     float2 av[RTP][C::PT];
-    // G and out' at the distance window (same for every offset)
-    float gu[C::RD][C::PD], ou[C::RD][C::PD];
+    // (G, out') at the distance window (same for every offset)
+    float2 gref[RD][PD];
 #pragma unroll
     for (int rp = 0; rp < RTP; ++rp)
 #pragma unroll
@@ -151,25 +206,23 @@ __global__ void __launch_bounds__(32 * NW, 1)
             av[rp][p] = make_float2(vt[i], vt[i + C::BX]);
         }
 #pragma unroll
-    for (int r = 0; r < C::RD; ++r)
+    for (int r = 0; r < RD; ++r)
 #pragma unroll
-        for (int p = 0; p < C::PD; ++p) {
-            const int i = (sz + p - N) * C::PLANE + (sy + r - N) * C::BX + sx;
-            gu[r][p] = gt[i];
-            ou[r][p] = ot[i];
-        }
+        for (int p = 0; p < PD; ++p) gref[r][p] = got[(sz + p - N) * C::PLANE + (sy + r - N) * C::BX + sx];
     auto avs = [&](int r, int p) { return (r & 1) ? av[r >> 1][p].y : av[r >> 1][p].x; };
 
-    float acc[RY][RZ];
+    // gpad' = acc_e + (-2 ln2) acc_t: the G(q+o) e_q(o) terms and the t A terms
+    float acc_e[RY][RZ], acc_t[RY][RZ];
 #pragma unroll
     for (int r = 0; r < RY; ++r)
 #pragma unroll
-        for (int q = 0; q < RZ; ++q) acc[r][q] = 0.f;
+        for (int q = 0; q < RZ; ++q) acc_e[r][q] = acc_t[r][q] = 0.f;
     double hacc = 0.0;
     const float2 minus1 = make_float2(-1.f, -1.f);
 
-    for (int oz = -M; oz <= M; ++oz) {
-        for (int oy = -M; oy <= M; ++oy) {
+    for (int run = run0; run < run1; ++run) {
+        const int oz = run / (2 * M + 1) - M, oy = run % (2 * M + 1) - M;
+        {
             // dL/dh terms of this run of 2M+1 offsets, summed in FP32, then added to
             // the FP64 total once per run
             float hrun = 0.f;
@@ -177,7 +230,7 @@ __global__ void __launch_bounds__(32 * NW, 1)
                 const int off = oz * C::PLANE + oy * C::BX + ox;
                 // differences t = v'_u - v'_{u+o} over the window (row pairs), candidates b
                 float2 t2[RTP][C::PT];
-                float bv[C::RD][C::PD];
+                float bv[RD][PD];
 #pragma unroll
                 for (int rp = 0; rp < RTP; ++rp)
 #pragma unroll
@@ -187,99 +240,126 @@ __global__ void __launch_bounds__(32 * NW, 1)
                         const float b0 = vt[i], b1 = vt[i + C::BX];
                         t2[rp][p] = __ffma2_rn(make_float2(b0, b1), minus1, av[rp][p]);
                         const int r0 = 2 * rp, r1 = 2 * rp + 1;
-                        if (p >= N && p < N + C::PD) {
-                            if (r0 >= N && r0 < N + C::RD) bv[r0 - N][p - N] = b0;
-                            if (r1 >= N && r1 < N + C::RD) bv[r1 - N][p - N] = b1;
+                        if (p >= N && p < N + PD) {
+                            if (r0 >= N && r0 < N + RD) bv[r0 - N][p - N] = b0;
+                            if (r1 >= N && r1 < N + RD) bv[r1 - N][p - N] = b1;
                         }
                     }
                 auto ts = [&](int r, int p) { return (r & 1) ? t2[r >> 1][p].y : t2[r >> 1][p].x; };
-                // distance D' on the distance window: z sums of t^2 (packed row pairs),
-                // then y sums, then x across lanes
-                float2 zs[RTP][C::PD];
+                // distance D' on the distance window: z sums of t^2 (sliding window over
+                // packed row pairs), y sums (pairs of rows share the middle terms), x
+                // across lanes (adds packed over pairs of planes)
+                float zrow[C::RT][PD];
 #pragma unroll
-                for (int rp = 0; rp < RTP; ++rp)
+                for (int rp = 0; rp < RTP; ++rp) {
+                    float2 run = __fmul2_rn(t2[rp][0], t2[rp][0]);
 #pragma unroll
-                    for (int p = 0; p < C::PD; ++p) {
-                        float2 sum = __fmul2_rn(t2[rp][p], t2[rp][p]);
+                    for (int k = 1; k < K; ++k) run = __ffma2_rn(t2[rp][k], t2[rp][k], run);
+                    zrow[2 * rp][0] = run.x;
+                    zrow[2 * rp + 1][0] = run.y;
 #pragma unroll
-                        for (int kz = 1; kz < C::K; ++kz)
-                            sum = __ffma2_rn(t2[rp][p + kz], t2[rp][p + kz], sum);
-                        zs[rp][p] = sum;
+                    for (int p = 1; p < PD; ++p) {
+                        const float2 tn = t2[rp][p + K - 1], to = t2[rp][p - 1];
+                        run = __ffma2_rn(tn, tn, run);
+                        run = __ffma2_rn(make_float2(-to.x, -to.y), to, run);
+                        zrow[2 * rp][p] = run.x;
+                        zrow[2 * rp + 1][p] = run.y;
                     }
-                auto zss = [&](int r, int p) { return (r & 1) ? zs[r >> 1][p].y : zs[r >> 1][p].x; };
-                float D[C::RD][C::PD];
+                }
+                float D[RD][PD];
 #pragma unroll
-                for (int r = 0; r < C::RD; ++r)
+                for (int p = 0; p < PD; ++p) {
+                    float col[C::RT], dcol[RD];
 #pragma unroll
-                    for (int p = 0; p < C::PD; ++p) {
-                        float sum = zss(r, p);
+                    for (int r = 0; r < C::RT; ++r) col[r] = zrow[r][p];
+                    box_pairs<K, RD>(col, dcol);
 #pragma unroll
-                        for (int ky = 1; ky < C::K; ++ky) sum += zss(r + ky, p);
-                        D[r][p] = sum;
+                    for (int r = 0; r < RD; ++r) D[r][p] = dcol[r];
+                }
+#pragma unroll
+                for (int r = 0; r < RD; ++r)
+#pragma unroll
+                    for (int p = 0; p < PD; p += 2) {
+                        const float2 x2 = xbox_pair<N>(make_float2(D[r][p], D[r][p + 1]));
+                        D[r][p] = x2.x;
+                        D[r][p + 1] = x2.y;
                     }
+                // weights, (G, out') at u+o, and the field a_o(u) (without the -ln2);
+                // gd = G(u) (v'_{u+o} - out'_u) is shared with the dL/dh term
+                float e[RD][PD], a[RD][PD], gd[RD][PD], guo[RD][PD];
 #pragma unroll
-                for (int r = 0; r < C::RD; ++r)
+                for (int r = 0; r < RD; ++r)
 #pragma unroll
-                    for (int p = 0; p < C::PD; ++p) {
-                        D[r][p] = xbox_lanes<N>(D[r][p]);
-                    }
-                // weights, G(u+o), and the field a_o(u) (without the -ln2)
-                float e[C::RD][C::PD], a[C::RD][C::PD], guo[C::RD][C::PD];
-#pragma unroll
-                for (int r = 0; r < C::RD; ++r)
-#pragma unroll
-                    for (int p = 0; p < C::PD; ++p) {
+                    for (int p = 0; p < PD; ++p) {
                         const int i = (sz + p - N) * C::PLANE + (sy + r - N) * C::BX + sx + off;
-                        const float g2 = gt[i], o2 = ot[i];
+                        const float2 go2 = got[i];
                         e[r][p] = ex2_neg(D[r][p]);
-                        guo[r][p] = g2;
+                        guo[r][p] = go2.x;
                         const float vu = avs(r + N, p + N);
-                        a[r][p] = e[r][p] * fmaf(gu[r][p], bv[r][p] - ou[r][p], g2 * (vu - o2));
+                        gd[r][p] = gref[r][p].x * (bv[r][p] - gref[r][p].y);
+                        a[r][p] = e[r][p] * fmaf(go2.x, vu - go2.y, gd[r][p]);
                     }
-                // box sum of a over the patch: z, then y, then x across lanes
-                float za[C::RD][RZ];
+                // box sum of a over the patch: z, then y (pairs share the middle terms),
+                // then x across lanes
+                float za[RD][RZ];
 #pragma unroll
-                for (int r = 0; r < C::RD; ++r)
+                for (int r = 0; r < RD; ++r) box_pairs<K, RZ>(a[r], za[r]);
 #pragma unroll
-                    for (int q = 0; q < RZ; ++q) {
-                        float sum = a[r][q];
+                for (int q = 0; q < RZ; q += 2) {
+                    float c0[RD], c1[RD], y0[RY], y1[RY];
 #pragma unroll
-                        for (int kz = 1; kz < C::K; ++kz) sum += a[r][q + kz];
-                        za[r][q] = sum;
+                    for (int r = 0; r < RD; ++r) {
+                        c0[r] = za[r][q];
+                        c1[r] = za[r][q + 1];
                     }
+                    box_pairs<K, RY>(c0, y0);
+                    box_pairs<K, RY>(c1, y1);
 #pragma unroll
-                for (int r = 0; r < RY; ++r)
+                    for (int r = 0; r < RY; ++r) {
+                        const float2 xv = xbox_pair<N>(make_float2(y0[r], y1[r]));
 #pragma unroll
-                    for (int q = 0; q < RZ; ++q) {
-                        float yv = za[r][q];
-#pragma unroll
-                        for (int ky = 1; ky < C::K; ++ky) yv += za[r + ky][q];
-                        const float xv = xbox_lanes<N>(yv);
-                        // gpad' += G(q+o) e_q(o) + 2 (v'_q - v'_{q+o}) (-ln2) A(q)
-                        acc[r][q] = fmaf(guo[r + N][q + N], e[r + N][q + N], acc[r][q]);
-                        acc[r][q] = fmaf(-2.f * kLn2 * ts(r + 2 * N, q + 2 * N), xv, acc[r][q]);
-                        // dL/dh partial: a1_o(q) D'_q(o), a1 = -ln2 e G(q) (v'_{q+o} - out'_q)
-                        const float a1 = e[r + N][q + N] * gu[r + N][q + N] *
-                                         (bv[r + N][q + N] - ou[r + N][q + N]);
-                        hrun = fmaf(a1, D[r + N][q + N], hrun);
+                        for (int h = 0; h < 2; ++h) {
+                            const int qq = q + h;
+                            const float A = h ? xv.y : xv.x;
+                            // gpad' += G(q+o) e_q(o) + 2 (v'_q - v'_{q+o}) (-ln2) A(q)
+                            acc_e[r][qq] = fmaf(guo[r + N][qq + N], e[r + N][qq + N], acc_e[r][qq]);
+                            acc_t[r][qq] = fmaf(ts(r + 2 * N, qq + 2 * N), A, acc_t[r][qq]);
+                            // dL/dh partial: a1_o(q) D'_q(o), a1 = -ln2 e G(q) (v'_{q+o} - out'_q)
+                            hrun = fmaf(e[r + N][qq + N] * gd[r + N][qq + N], D[r + N][qq + N], hrun);
+                        }
                     }
+                }
             }
             hacc += (double)hrun;
         }
     }
+    float acc[RY][RZ];
+#pragma unroll
+    for (int r = 0; r < RY; ++r)
+#pragma unroll
+        for (int q = 0; q < RZ; ++q) acc[r][q] = fmaf(-2.f * kLn2, acc_t[r][q], acc_e[r][q]);
 
-    // store gpad' for the thread's padded-domain voxels; reduce the h partial
-    const int px = blockIdx.x * C::XO + lane - 2 * N;  // staged x of this lane
+    // store gpad' for the thread's padded-domain voxels (or this part's partial
+    // brick, every lane); reduce the h partial
+    const int px = bx * C::XO + lane - 2 * N;  // staged x of this lane
     const bool lane_ok = lane >= 2 * N && lane < 32 - 2 * N && px < Xp;
     double hsum = 0.0;
+    if (nparts == 1) {
 #pragma unroll
-    for (int q = 0; q < RZ; ++q) {
-        const int pz = Z0 + q;
+        for (int q = 0; q < RZ; ++q) {
+            const int pz = Z0 + q;
 #pragma unroll
-        for (int r = 0; r < RY; ++r) {
-            const int py = Y0 + warp * RY + r;
-            if (lane_ok && py < Ypd && pz < Zp) gpad[((size_t)pz * Yp + py) * Xs + px] = acc[r][q];
+            for (int r = 0; r < RY; ++r) {
+                const int py = Y0 + warp * RY + r;
+                if (lane_ok && py < Ypd && pz < Zp) gpad[((size_t)pz * Yp + py) * Xs + px] = acc[r][q];
+            }
         }
+    } else {
+        float* brick = tl.side + ((size_t)part * tl.ntail + (tile - tl.full)) * C::TILE_VOX;
+#pragma unroll
+        for (int q = 0; q < RZ; ++q)
+#pragma unroll
+            for (int r = 0; r < RY; ++r) brick[(q * C::TY + warp * RY + r) * 32 + lane] = acc[r][q];
     }
     // Halo lanes duplicate a neighbouring CTA's voxels: only output lanes count.
     // Voxels outside the volume (padding, rows/planes past the end) have G = 0 and
@@ -291,7 +371,25 @@ __global__ void __launch_bounds__(32 * NW, 1)
     if (threadIdx.x == 0) {
         double s = 0.0;
         for (int w = 0; w < NW; ++w) s += red[w];
-        hpart[((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = -kLn2 * s;
+        hpart[blockIdx.x] = -kLn2 * s;
+    }
+}
+
+// gpad' of the tail tiles: the sum of their S partial bricks, in part order.
+template <int N, int RZ, int TY, int XO>
+__global__ void __launch_bounds__(256) adj_tail_combine_kernel(const AdjTail tl, int Xp, int Ypd,
+                                                               int Zp, int Xs, int Yp,
+                                                               float* __restrict__ gpad) {
+    constexpr int TILE_VOX = RZ * TY * 32;
+    const int t = blockIdx.x, tile = tl.full + t;
+    const int bx = tile % tl.nx, by = (tile / tl.nx) % tl.ny, bz = tile / (tl.nx * tl.ny);
+    for (int k = threadIdx.x; k < TILE_VOX; k += blockDim.x) {
+        const int lane = k & 31, row = (k >> 5) % TY, q = (k >> 5) / TY;
+        const int px = bx * XO + lane - 2 * N, py = by * TY + row, pz = bz * RZ + q;
+        if (lane < 2 * N || lane >= 32 - 2 * N || px >= Xp || py >= Ypd || pz >= Zp) continue;
+        float sum = 0.f;
+        for (int p = 0; p < tl.S; ++p) sum += tl.side[((size_t)p * tl.ntail + t) * TILE_VOX + k];
+        gpad[((size_t)pz * Yp + py) * Xs + px] = sum;
     }
 }
 
@@ -338,38 +436,76 @@ __global__ void adj_hgrad_kernel(const double* __restrict__ hpart, int n, double
     }
 }
 
+// Tail split bounds: S * ntail <= min(SMs, kAdjMaxTailCtas), S <= kAdjMaxParts.
+constexpr int kAdjMaxTailCtas = 1024;
+constexpr int kAdjMaxParts = 16;
+
+// With one CTA per SM, n tiles fill n / SMs whole waves; the tiles of a last,
+// partial wave are split into S parts of their offset runs so that the tail wave
+// holds S * ntail <= SMs CTAs of 1/S of the work.
+static AdjTail adj_tail_plan(int nx, int ny, int nz, int runs) {
+    AdjTail t{};
+    t.nx = nx;
+    t.ny = ny;
+    const int n = nx * ny * nz;
+    const int slots = std::min(device_sm_count(), kAdjMaxTailCtas);
+    const int tail = n % slots;
+    const int S = tail ? std::min(std::min(slots / tail, runs), kAdjMaxParts) : 1;
+    if (S < 2) {
+        t.full = n;
+        t.S = 1;
+        t.ntail = 0;
+    } else {
+        t.full = n - tail;
+        t.S = S;
+        t.ntail = tail;
+    }
+    return t;
+}
+
 template <int M, int N, int RY, int RZ, int NW>
 static cudaError_t run_adj3d(const Staging& st, const void* staged, const float* d_out,
                              const float* d_zsum, const float* d_gout, float s, float h,
-                             float* gin, double* hgrad, float* G, float* O, float* gpad,
-                             double* hpart, unsigned int* errword, cudaStream_t stream) {
+                             float* gin, double* hgrad, float2* GO, float* gpad,
+                             double* hpart, float* side, unsigned int* errword,
+                             cudaStream_t stream) {
     using C = Adj3d<M, N, RY, RZ, NW>;
     dim3 rows(st.Yp, st.Zp);
     adj_aux_kernel<<<rows, 256, 0, stream>>>(d_gout, d_out, d_zsum, st.X, st.Y, st.Z, st.H, st.Xs,
-                                              st.Yp, s, G, O);
+                                              st.Yp, s, GO);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    CUtensorMap vmap, gmap, omap;
+    CUtensorMap vmap, gomap;
     const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
     const uint64_t strides[2] = {(uint64_t)st.Xs * 4, (uint64_t)st.Xs * st.Yp * 4};
     const uint32_t box[3] = {(uint32_t)C::BX, (uint32_t)C::BY, (uint32_t)C::BZ};
+    // (G, out') pairs: the same geometry with twice the floats per row
+    const uint64_t dims2[3] = {2 * (uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
+    const uint64_t strides2[2] = {(uint64_t)st.Xs * 8, (uint64_t)st.Xs * st.Yp * 8};
+    const uint32_t box2[3] = {2 * (uint32_t)C::BX, (uint32_t)C::BY, (uint32_t)C::BZ};
     if ((e = encode_tensor_map(&vmap, false, 3, dims, strides, box, const_cast<void*>(staged))))
         return e;
-    if ((e = encode_tensor_map(&gmap, false, 3, dims, strides, box, G))) return e;
-    if ((e = encode_tensor_map(&omap, false, 3, dims, strides, box, O))) return e;
+    if ((e = encode_tensor_map(&gomap, false, 3, dims2, strides2, box2, GO))) return e;
     auto kern = nlm3d_adj_kernel<M, N, RY, RZ, NW>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES)))
         return e;
-    dim3 grid((st.Xp + C::XO - 1) / C::XO, (st.Yp + C::TY - 1) / C::TY, (st.Zp + RZ - 1) / RZ);
-    kern<<<grid, 32 * NW, C::SMEM_BYTES, stream>>>(vmap, gmap, omap, st.X, st.Y, st.Z, st.Xs,
-                                                   st.Yp, gpad, hpart, errword);
+    AdjTail tl = adj_tail_plan((st.Xp + C::XO - 1) / C::XO, (st.Yp + C::TY - 1) / C::TY,
+                               (st.Zp + RZ - 1) / RZ, (2 * M + 1) * (2 * M + 1));
+    tl.side = side;
+    const int nblk = tl.full + tl.S * tl.ntail;
+    kern<<<nblk, 32 * NW, C::SMEM_BYTES, stream>>>(vmap, gomap, st.X, st.Y, st.Z, st.Xs, st.Yp,
+                                                   gpad, hpart, tl, errword);
     if ((e = cudaGetLastError())) return e;
+    if (tl.ntail > 0) {
+        adj_tail_combine_kernel<N, RZ, C::TY, C::XO><<<tl.ntail, 256, 0, stream>>>(
+            tl, st.Xp, st.Yp, st.Zp, st.Xs, st.Yp, gpad);
+        if ((e = cudaGetLastError())) return e;
+    }
     dim3 out_rows(st.Y, st.Z);
     adj_fold_kernel<<<out_rows, 128, 0, stream>>>(gpad, st.X, st.Y, st.Z, st.H, st.Xs, st.Yp, s,
                                                   gin);
     if ((e = cudaGetLastError())) return e;
     if (hgrad) {
-        const int nblk = grid.x * grid.y * grid.z;
         adj_hgrad_kernel<<<1, 32, 0, stream>>>(hpart, nblk, -2.0 / (double)h, hgrad);
         e = cudaGetLastError();
     }
@@ -395,14 +531,25 @@ bool nlm3d_adj_supported(int sr, int pr) {
     return false;
 }
 
-// Number of CTAs of the adjoint kernel (one double of h partials each).
+// Upper bound on the CTAs of the adjoint kernel (one double of h partials each):
+// the tiles plus at most kAdjMaxTailCtas tail-part CTAs.
 size_t adj3d_ctas(const Staging& st, int sr, int pr) {
 #define X_(m, n)                                                                             \
     if (sr == m && pr == n) {                                                                \
         using C = AdjShape<m, n>::C;                                                         \
         return (size_t)((st.Xp + C::XO - 1) / C::XO) * ((st.Yp + C::TY - 1) / C::TY) *     \
-               ((st.Zp + AdjShape<m, n>::RZ - 1) / AdjShape<m, n>::RZ);                      \
+                   ((st.Zp + AdjShape<m, n>::RZ - 1) / AdjShape<m, n>::RZ) +                 \
+               kAdjMaxTailCtas;                                                              \
     }
+    GNLM_ADJ3D_CASES(X_)
+#undef X_
+    return 0;
+}
+
+// Bytes of the tail parts' partial bricks.
+size_t adj3d_side_bytes(int sr, int pr) {
+#define X_(m, n) \
+    if (sr == m && pr == n) return (size_t)kAdjMaxTailCtas * AdjShape<m, n>::C::TILE_VOX * 4;
     GNLM_ADJ3D_CASES(X_)
 #undef X_
     return 0;
@@ -410,14 +557,15 @@ size_t adj3d_ctas(const Staging& st, int sr, int pr) {
 
 cudaError_t launch_nlm3d_adj(const Staging& st, const void* staged, const float* d_out,
                              const float* d_zsum, const float* d_gout, int sr, int pr, float s,
-                             float h, float* gin, double* hgrad, float* G, float* O, float* gpad,
-                             double* hpart, unsigned int* errword, cudaStream_t stream) {
+                             float h, float* gin, double* hgrad, float2* GO, float* gpad,
+                             double* hpart, float* side, unsigned int* errword,
+                             cudaStream_t stream) {
     if (st.H > kMaxHalo) return cudaErrorNotSupported;
 #define X_(m, n)                                                                                \
     if (sr == m && pr == n)                                                                     \
         return run_adj3d<m, n, AdjShape<m, n>::RY, AdjShape<m, n>::RZ, AdjShape<m, n>::NW>(    \
-            st, staged, d_out, d_zsum, d_gout, s, h, gin, hgrad, G, O, gpad, hpart, errword,    \
-            stream);
+            st, staged, d_out, d_zsum, d_gout, s, h, gin, hgrad, GO, gpad, hpart, side,         \
+            errword, stream);
     GNLM_ADJ3D_CASES(X_)
 #undef X_
     return cudaErrorNotSupported;

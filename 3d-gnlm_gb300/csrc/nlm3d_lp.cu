@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(256) lp_combine_kernel(const float2* __restric
     }
 }
 
-static int sm_count() {
+int device_sm_count() {
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
@@ -38,7 +38,7 @@ static int sm_count() {
 int nlm3d_lp_split(int X, int Y, int Z, int tz) {
     if (tz <= 0) return 1;
     const long long n = (long long)((X + 31) / 32) * ((Y + 15) / 16) * ((Z + tz - 1) / tz);
-    const long long sms = sm_count();
+    const long long sms = device_sm_count();
     const double one = (double)((n + sms - 1) / sms);
     const double two = (double)((2 * n + sms - 1) / sms) / 2.0;
     return two < 0.97 * one ? 2 : 1;
@@ -85,7 +85,7 @@ static cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     const size_t plane = (size_t)st.X * st.Y;
     const size_t v0 = (size_t)zc0 * tz * plane;
     const size_t v1 = (size_t)std::min(zc1 * tz, st.Z) * plane;
-    const size_t blocks = std::min<size_t>((v1 - v0 + 255) / 256, (size_t)sm_count() * 8);
+    const size_t blocks = std::min<size_t>((v1 - v0 + 255) / 256, (size_t)device_sm_count() * 8);
     lp_combine_kernel<<<(unsigned)blocks, 256, 0, stream>>>(acc, a.part_stride, v0, v1 - v0,
                                                             inv_scale, out, zsum);
     return cudaGetLastError();

@@ -386,7 +386,8 @@ int nlm2d_forward(const void* d_in, int in_dtype, int X, int Y, int sr, int pr, 
 size_t nlm3d_adjoint_workspace_bytes(int X, int Y, int Z, int sr, int pr) {
     if (X < 1 || Y < 1 || Z < 1 || sr < 0 || pr < 0 || !nlm3d_adj_supported(sr, pr)) return 0;
     const Staging st = make_staging(X, Y, Z, sr + pr, sr + pr, false);
-    return 4 * st.bytes() + align_up(adj3d_ctas(st, sr, pr) * sizeof(double), kAlign);
+    return 4 * st.bytes() + align_up(adj3d_ctas(st, sr, pr) * sizeof(double), kAlign) +
+           align_up(adj3d_side_bytes(sr, pr), kAlign);
 }
 
 int nlm3d_adjoint(const float* d_in, const float* d_out, const float* d_zsum, const float* d_gout,
@@ -405,15 +406,16 @@ int nlm3d_adjoint(const float* d_in, const float* d_out, const float* d_zsum, co
         return rc;
     char* base = static_cast<char*>(d_ws);
     void* staged = base;
-    float* G = reinterpret_cast<float*>(base + st.bytes());
-    float* O = reinterpret_cast<float*>(base + 2 * st.bytes());
+    float2* GO = reinterpret_cast<float2*>(base + st.bytes());  // 2 * st.bytes()
     float* gpad = reinterpret_cast<float*>(base + 3 * st.bytes());
     double* hpart = reinterpret_cast<double*>(base + 4 * st.bytes());
+    float* side = reinterpret_cast<float*>(
+        base + 4 * st.bytes() + align_up(adj3d_ctas(st, sr, pr) * sizeof(double), kAlign));
     const float s = weight_scale(pr, 3, h);
     cudaError_t e = launch_stage(d_in, NLM_F32, false, s, st, staged, stream);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint staging");
-    e = launch_nlm3d_adj(st, staged, d_out, d_zsum, d_gout, sr, pr, s, h, d_gin, d_hgrad, G, O,
-                         gpad, hpart, device_error_word(), stream);
+    e = launch_nlm3d_adj(st, staged, d_out, d_zsum, d_gout, sr, pr, s, h, d_gin, d_hgrad, GO,
+                         gpad, hpart, side, device_error_word(), stream);
     if (e != cudaSuccess) return cuda_fail(e, "nlm3d_adjoint launch");
     return NLM_OK;
 }

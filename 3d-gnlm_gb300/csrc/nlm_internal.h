@@ -74,14 +74,20 @@ cudaError_t launch_nlm3d_lp(const Staging& st, const void* staged, int sr, int p
                             float inv_scale, float* out, float* zsum, float2* acc,
                             unsigned int* errword, cudaStream_t stream, int zc0, int zc1);
 
-// 3D adjoint (see nlm3d_adj.cu).  Scratch: G, out', gpad' (each st.bytes()) and
-// adj3d_ctas() doubles of h partial sums.
+// 3D adjoint (see nlm3d_adj.cu).  Scratch: (G, out') pairs (2 st.bytes()), gpad'
+// (st.bytes()), adj3d_ctas() doubles of h partial sums and adj3d_side_bytes() of
+// partial bricks of split tail tiles.
 bool nlm3d_adj_supported(int sr, int pr);
 size_t adj3d_ctas(const Staging& st, int sr, int pr);
+size_t adj3d_side_bytes(int sr, int pr);
 cudaError_t launch_nlm3d_adj(const Staging& st, const void* staged, const float* d_out,
                              const float* d_zsum, const float* d_gout, int sr, int pr, float s,
-                             float h, float* gin, double* hgrad, float* G, float* O, float* gpad,
-                             double* hpart, unsigned int* errword, cudaStream_t stream);
+                             float h, float* gin, double* hgrad, float2* GO, float* gpad,
+                             double* hpart, float* side, unsigned int* errword,
+                             cudaStream_t stream);
+
+// Multiprocessors of the current device (1 if it cannot be queried).
+int device_sm_count();
 
 // Tile-shape variant the forward uses for (dims, sr, pr, fp16): the autotuned
 // choice if one was recorded, else default_variant().
