@@ -176,10 +176,19 @@ def cpu_baseline(shape, budget_s=10.0):
     t0 = time.perf_counter()
     O.nlm3d(slab, SR, PR, H)
     dt = time.perf_counter() - t0
+    # the same port on one thread, on a thinner slab
+    O.set_threads(1)
+    slab1 = np.ascontiguousarray(vol[Z // 2 - 2:Z // 2 + 2])
+    t1 = time.perf_counter()
+    O.nlm3d(slab1, SR, PR, H)
+    dt1 = time.perf_counter() - t1
+    O.set_threads(threads)
     return {"value": round(nz * Y * X / dt / 1e6, 3), "unit": UNIT, "cores": threads,
             "kind": "port",
+            "single_thread_value": round(slab1.size / dt1 / 1e6, 3),
             "sample": f"z-slab {nz}x{Y}x{X} of the 256^3 volume, oracle FP32 separable form "
-                      f"(reflect borders at the slab ends), {dt:.1f} s"}
+                      f"(reflect borders at the slab ends), {dt:.1f} s; single thread: "
+                      f"z-slab 4x{Y}x{X}, {dt1:.1f} s"}
 
 
 def bench_batched(torch, gnlm, reps=3):
