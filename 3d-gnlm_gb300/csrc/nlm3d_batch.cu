@@ -417,14 +417,19 @@ int nlm3d_batch_autotune(nlm_batch_plan* p, float* times_ms, nlm_stream_t stream
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    auto done = [&](int rc) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+    };
     for (int v = 0; v < kBatchVariants; ++v) {
         int rc = nlm3d_batch_set_variant(p, v);
-        if (rc != NLM_OK) return rc;
+        if (rc != NLM_OK) return done(rc);
         float ms = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             cudaEventRecord(e0, stream);
             rc = nlm3d_batch_run(p, stream_);
-            if (rc != NLM_OK) return rc;
+            if (rc != NLM_OK) return done(rc);
             cudaEventRecord(e1, stream);
             cudaEventSynchronize(e1);
             float t = 0.f;
@@ -437,8 +442,7 @@ int nlm3d_batch_autotune(nlm_batch_plan* p, float* times_ms, nlm_stream_t stream
             best_ms = ms;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    done(NLM_OK);
     int rc = nlm3d_batch_set_variant(p, best);
     return rc == NLM_OK ? best : rc;
 }
@@ -457,6 +461,21 @@ int nlm3d_batch_destroy(nlm_batch_plan* p) {
     if (!p) return NLM_OK;
     cudaDeviceSynchronize();
     free_plan(p);
+    return NLM_OK;
+}
+
+int nlm3d_forward_batched(const nlm_volume* vols, int n, nlm_stream_t stream) {
+    nlm_batch_plan* p = nullptr;
+    int rc = nlm3d_batch_create(vols, n, 0, &p);
+    if (rc != NLM_OK) return rc;
+    rc = nlm3d_batch_run(p, stream);
+    const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    nlm3d_batch_destroy(p);
+    if (rc != NLM_OK) return rc;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(NLM_ERR_CUDA, "batched forward failed");
+    }
     return NLM_OK;
 }
 

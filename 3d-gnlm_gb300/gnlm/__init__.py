@@ -83,6 +83,7 @@ def lib():
     L.nlm3d_batch_set_variant.argtypes = [vp, i]
     L.nlm3d_batch_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(sz)]
     L.nlm3d_batch_destroy.argtypes = [vp]
+    L.nlm3d_forward_batched.argtypes = [ctypes.POINTER(NLMVolume), i, vp]
     L.nlm_variant_count.argtypes = [i, u]
     L.nlm_set_variant.argtypes = [i, i, i, u, i]
     L.nlm_get_variant.argtypes = [i, i, i, u]
@@ -208,6 +209,22 @@ def nlm3d_adjoint(x, out, zsum, gout, sr, pr, h, gin=None, hgrad=None, workspace
                               float(h), _ptr(gin), _ptr(hgrad), ws_ptr, ws_bytes,
                               _stream_ptr(stream)))
     return gin, hgrad
+
+
+def nlm3d_forward_batched(volumes, stream=None):
+    """One-shot batched forward (plan built, run once and freed; synchronous).
+
+    ``volumes`` is a list of (tensor [Z, Y, X], sr, pr, h); returns the outputs."""
+    torch = _torch()
+    inputs = [v[0].contiguous() for v in volumes]
+    outputs = [torch.empty(t.shape, dtype=torch.float32, device=t.device) for t in inputs]
+    arr = (NLMVolume * len(volumes))()
+    for k, ((_, sr, pr, h), x, o) in enumerate(zip(volumes, inputs, outputs)):
+        Z, Y, X = x.shape
+        arr[k] = NLMVolume(x.data_ptr(), _dtype_code(x), X, Y, Z, sr, pr, float(h), o.data_ptr(),
+                           None)
+    check(lib().nlm3d_forward_batched(arr, len(volumes), _stream_ptr(stream)))
+    return outputs
 
 
 class BatchPlan:

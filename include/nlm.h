@@ -196,6 +196,10 @@ int nlm3d_batch_autotune(nlm_batch_plan* plan, float* times_ms, nlm_stream_t str
 int nlm3d_batch_set_variant(nlm_batch_plan* plan, int variant);
 int nlm3d_batch_info(const nlm_batch_plan* plan, int* n_items, int* variant, size_t* device_bytes);
 int nlm3d_batch_destroy(nlm_batch_plan* plan);
+/* One-shot form of the above (no counterpart in the reference): builds a plan
+ * with the default tile shape, runs it once on `stream`, waits for it and frees
+ * it.  Synchronous; callers that denoise the same batch repeatedly keep a plan. */
+int nlm3d_forward_batched(const nlm_volume* vols, int n, nlm_stream_t stream);
 
 /* ------------------------------------------------------------ autotuner -- */
 

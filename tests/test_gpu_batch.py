@@ -102,3 +102,23 @@ def test_batch_rejects_unsupported(torch_cuda, gnlm_lib):
     with pytest.raises(gnlm_lib.NLMError) as ei:
         gnlm_lib.BatchPlan([(x, 3, 2, 0.05)])
     assert ei.value.code == gnlm_lib.NLM_ERR_UNSUPPORTED
+
+
+def test_one_shot_batched_forward_equals_plan(torch_cuda, gnlm_lib):
+    """nlm3d_forward_batched (plan built, run once, freed) gives the plan's bits and
+    rejects what nlm3d_batch_create rejects."""
+    torch = torch_cuda
+    vols, hosts = _volumes(torch, SPECS[:5])
+    plan = gnlm_lib.BatchPlan(vols)
+    try:
+        ref = [o.clone() for o in plan.run()]
+        torch.cuda.synchronize()
+    finally:
+        plan.close()
+    outs = gnlm_lib.nlm3d_forward_batched(vols)
+    for o, r in zip(outs, ref):
+        assert torch.equal(o, r)
+    with pytest.raises(gnlm_lib.NLMError) as ei:
+        gnlm_lib.nlm3d_forward_batched([(vols[0][0], 3, 2, 0.05)])
+    assert ei.value.code == gnlm_lib.NLM_ERR_UNSUPPORTED
+    assert gnlm_lib.device_status() == (0, 0)
