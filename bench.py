@@ -42,6 +42,13 @@ SR, PR, H = 3, 1, 0.05
 N_ELLIPSOIDS, SIGMA, SEED = 64, 0.05, 2
 OFFSETS = (2 * SR + 1) ** 3
 FLOPS_PER_PAIR = 12  # diff, square, 6 box-sum add/sub, scale, Z add, num FMA (2)
+# Adjoint, per (padded voxel, offset): distance recomputed (diff, square, 6 box-sum
+# add/sub, scale = 9); a = e [G(u)(v'(u+o) - out'(u)) + G(u+o)(v'(u) - out'(u+o))]
+# (2 differences, 2 products, 1 add, times e = 6); box sum of a (6 add/sub); gathered
+# terms G(q+o) e + (-2 ln2) t A (FMA 2, product + FMA 3 = 5); dL/dh term a1 D'
+# (product + FMA = 3).  The padded domain is the unit: halo gradients fold back
+# through REFLECT_101.
+ADJ_FLOPS_PER_PAIR = 29
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD_NAME = "nlm3d_256cubed_sr3_pr1_fp32"
 
@@ -292,9 +299,10 @@ def bench_large_patch(torch, gnlm, reps=3):
             "autotune_ms": [round(v, 3) for v in tune]}
 
 
-def bench_adjoint(torch, gnlm, steps=50):
-    """128^3 (ellipsoids, sigma 0.05, sr 3, pr 1): forward + adjoint per step, used
-    to fit h by gradient descent on the MSE to the clean phantom."""
+def bench_adjoint(torch, gnlm, peak_tflops, steps=50, reps=20):
+    """128^3 (ellipsoids, sigma 0.05, sr 3, pr 1): forward + adjoint per step (median
+    of `reps` device-timed pairs), then used to fit h by gradient descent on the MSE
+    to the clean phantom."""
     from gnlm import phantom
     noisy, clean = phantom.ellipsoid_phantom((128, 128, 128), n_ellipsoids=16, sigma=0.05, seed=4)
     x, c = torch.from_numpy(noisy).cuda(), torch.from_numpy(clean).cuda()
@@ -309,14 +317,20 @@ def bench_adjoint(torch, gnlm, steps=50):
         gnlm.nlm3d_forward(x, SR, PR, 0.05, out=out, zsum=zs, return_zsum=True)
         gnlm.nlm3d_adjoint(x, out, zs, g, SR, PR, 0.05, gin=gin, hgrad=hg, workspace=ws)
     torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    ev[0].record(stream)
-    gnlm.nlm3d_forward(x, SR, PR, 0.05, out=out, zsum=zs, return_zsum=True)
-    ev[1].record(stream)
-    gnlm.nlm3d_adjoint(x, out, zs, g, SR, PR, 0.05, gin=gin, hgrad=hg, workspace=ws)
-    ev[2].record(stream)
-    ev[2].synchronize()
-    fwd_ms, adj_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    fwd_t, adj_t = [], []
+    for _ in range(reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(stream)
+        gnlm.nlm3d_forward(x, SR, PR, 0.05, out=out, zsum=zs, return_zsum=True)
+        ev[1].record(stream)
+        gnlm.nlm3d_adjoint(x, out, zs, g, SR, PR, 0.05, gin=gin, hgrad=hg, workspace=ws)
+        ev[2].record(stream)
+        ev[2].synchronize()
+        fwd_t.append(ev[0].elapsed_time(ev[1]))
+        adj_t.append(ev[1].elapsed_time(ev[2]))
+    fwd_ms, adj_ms = statistics.median(fwd_t), statistics.median(adj_t)
+    padded = (128 + 2 * (SR + PR)) ** 3
+    adj_tflops = ADJ_FLOPS_PER_PAIR * OFFSETS * padded / (adj_ms * 1e-3) / 1e12
     # h fit: 50 steps of normalised gradient descent on MSE(out(h), clean)
 
     def fit_step(hh):
@@ -340,7 +354,11 @@ def bench_adjoint(torch, gnlm, steps=50):
     t1.synchronize()
     return {"shape": [128, 128, 128], "search_radius": SR, "patch_radius": PR,
             "fwd_ms": round(fwd_ms, 3), "adjoint_ms": round(adj_ms, 3),
-            "fwd_adjoint_ms_per_step": round(fwd_ms + adj_ms, 3),
+            "fwd_adjoint_ms_per_step": round(fwd_ms + adj_ms, 3), "timing": f"median of {reps}",
+            "adjoint_tflops": round(adj_tflops, 3),
+            "adjoint_frac_fp32_peak": round(adj_tflops / peak_tflops, 4) if peak_tflops else None,
+            "adjoint_algorithmic": f"{ADJ_FLOPS_PER_PAIR} flops x {OFFSETS} offsets x {padded} "
+                                   f"padded voxels (shared-memory bound: ncu in profiles/)",
             "h_fit": {"steps": steps, "h0": 0.02, "h": round(h, 4), "mse0": mse0, "mse": mse,
                       "ms_per_step_with_loss_readback": round(t0.elapsed_time(t1) / steps, 3)}}
 
@@ -485,7 +503,7 @@ def run_gnlm(args):
     peak = fp32_peak_tflops(torch)
     peak_x2 = fp32_peak_tflops(torch, packed=True)
     batched = bench_batched(torch, gnlm) if not args.skip_extra else None
-    adjoint = bench_adjoint(torch, gnlm) if not args.skip_extra else None
+    adjoint = bench_adjoint(torch, gnlm, peak) if not args.skip_extra else None
     image2d = bench_2d(torch, gnlm) if not args.skip_extra else None
     large = bench_large_patch(torch, gnlm) if not args.skip_extra else None
     fused_mean = statistics.mean(fused_ms)
