@@ -140,6 +140,14 @@ __host__ __device__ __forceinline__ int reflect101(int i, int n) {
     return i < n ? i : period - i;
 }
 
+// reflect101 with the common case first: one reflection on each side covers
+// -n < i < 2n - 1 with two compares and no division; other offsets fall back.
+__device__ __forceinline__ int reflect101_near(int i, int n) {
+    int r = i < 0 ? -i : i;
+    r = r >= n ? 2 * n - 2 - r : r;
+    return (unsigned)r < (unsigned)n ? r : reflect101(i, n);
+}
+
 // Sum of y over the lanes [l - N, l + N] (valid for lanes N .. 31 - N).  N = 1: two
 // shuffles; N = 2: three (from pair sums); wider windows are assembled from
 // power-of-two window sums, e.g. 11 = 8 + 2 + 1 takes 6 shuffles instead of 10.

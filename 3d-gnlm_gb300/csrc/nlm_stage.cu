@@ -8,6 +8,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "../../include/nlm.h"
 #include "nlm_device.cuh"
 #include "nlm_internal.h"
@@ -39,54 +41,7 @@ Staging make_staging_pairs(int X, int Y, int Z, int H) {
     return s;
 }
 
-// Row-pair layout: block = (pair k, plane, copy c); rows 2k+c and 2k+c+1.
-template <typename Tin, bool PREPADDED>
-__global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict__ in, int X, int Y,
-                                                          int Z, int H, int Xp, int Yp, int Xs,
-                                                          int Yq, size_t copy_elems, float scale,
-                                                          __half2* __restrict__ dst, int pz0) {
-    const int k = blockIdx.x, pz = blockIdx.y + pz0, c = blockIdx.z;
-    const int r0 = 2 * k + c, r1 = r0 + 1;
-    __half2* drow = dst + c * copy_elems + ((size_t)pz * Yq + k) * Xs;
-    const Tin *s0 = nullptr, *s1 = nullptr;
-    if (PREPADDED) {
-        if (r0 < Yp) s0 = in + ((size_t)pz * Yp + r0) * Xp;
-        if (r1 < Yp) s1 = in + ((size_t)pz * Yp + r1) * Xp;
-    } else {
-        const int sz = reflect101(pz - H, Z);
-        if (r0 < Yp) s0 = in + ((size_t)sz * Y + reflect101(r0 - H, Y)) * X;
-        if (r1 < Yp) s1 = in + ((size_t)sz * Y + reflect101(r1 - H, Y)) * X;
-    }
-    for (int px = threadIdx.x; px < Xs; px += blockDim.x) {
-        float v0 = 0.f, v1 = 0.f;
-        if (px < Xp) {
-            const int sx = PREPADDED ? px : reflect101(px - H, X);
-            if (s0) v0 = to_f32(s0[sx]) * scale;
-            if (s1) v1 = to_f32(s1[sx]) * scale;
-        }
-        drow[px] = __floats2half2_rn(v0, v1);
-    }
-}
-
-template <typename Tin>
-static cudaError_t stage_pairs_typed(const void* in, bool prepadded, float scale, const Staging& st,
-                                     void* dst, cudaStream_t stream, int pz0, int pz1) {
-    dim3 grid(st.Yq, pz1 - pz0, 2);
-    const size_t copy_elems = st.copy_bytes() / 4;
-    if (prepadded)
-        stage_pairs_kernel<Tin, true><<<grid, 256, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp, st.Yp, st.Xs, st.Yq, copy_elems, scale,
-            (__half2*)dst, pz0);
-    else
-        stage_pairs_kernel<Tin, false><<<grid, 256, 0, stream>>>(
-            (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp, st.Yp, st.Xs, st.Yq, copy_elems, scale,
-            (__half2*)dst, pz0);
-    return cudaGetLastError();
-}
-
-// Warp per padded row (8 rows per 256-thread block, rows flattened over planes).
-// Each lane writes 16-byte vectors (4 FP32 or 8 FP16 values); columns inside the
-// volume map to the source row directly, only the 2H border columns reflect.
+// One 16-byte output chunk: 4 FP32 or 8 FP16 values.
 template <typename Tout>
 struct Vec16;
 template <>
@@ -144,90 +99,240 @@ __device__ __forceinline__ void load_vec(const Tin* p, float* v) {
     }
 }
 
-// VEC: every source row starts on a multiple of V::N elements and the halo H is one
-// too (not prepadded), so the chunks that lie inside the source row are one vector
-// load each; the 2H border columns and the stride padding take the scalar path.
-template <typename Tin, typename Tout, bool PREPADDED, bool VEC>
-__global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
-                                                    int Z, int H, int Hz, int Xp, int Yp,
-                                                    long long row0, long long row1, int Xs,
-                                                    float scale, Tout* __restrict__ dst) {
-    using V = Vec16<Tout>;
-    const long long row = row0 + (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (row >= row1) return;
-    const int lane = threadIdx.x & 31;
-    const int py = (int)(row % Yp), pz = (int)(row / Yp);
-    typename V::T* drow = reinterpret_cast<typename V::T*>(dst + row * Xs);
-    const Tin* srow;
-    if (PREPADDED) {
-        srow = in + row * Xp;
-    } else {
-        const int sz = reflect101(pz - Hz, Z);
-        const int sy = reflect101(py - H, Y);
-        srow = in + ((size_t)sz * Y + sy) * X;
-    }
+// Staging kernels, both layouts.  A warp copies whole padded rows: each lane owns
+// 16-byte output chunks c = lane, lane + 32, ... of a row and issues the loads of all
+// its chunks of kStageRows rows (kStageSlots per row and pass) before the first
+// store, so a warp keeps about 2 KB in flight.  Blocks stay resident (grid = SMs x
+// blocks per SM) and stride over row groups; a thread divides once, at the start,
+// and then advances its (row, plane) by adds.  Columns inside the volume map to the
+// source row directly (VEC: one vector load per chunk); only the 2H border columns
+// reflect, without divisions in the common case (reflect101_near).  Row indices are
+// 32-bit: the launcher splits launches to at most 2^30 rows.
+constexpr int kStageRows = 2;
+constexpr int kStageSlots = 3;  // a row of up to 96 chunks (1.5 KB) in one pass
+
+template <typename Tin, int NV, bool PREPADDED, bool VEC>
+__device__ __forceinline__ void stage_chunk(const Tin* srow, int px0, int X, int H, int Xp,
+                                            float* v) {
     const int sh = PREPADDED ? 0 : H;      // source column = padded column - sh
     const int slen = PREPADDED ? Xp : X;   // source row length
-    auto chunk = [&](int c, float* v) {
-        const int px0 = c * V::N;
-        if (VEC && px0 >= sh && px0 - sh + V::N <= slen) {
-            load_vec<Tin, V::N>(srow + (px0 - sh), v);
-        } else {
+    if (VEC && px0 >= sh && px0 - sh + NV <= slen) {
+        load_vec<Tin, NV>(srow + (px0 - sh), v);
+    } else {
 #pragma unroll
-            for (int i = 0; i < V::N; ++i) {
-                const int px = px0 + i;
-                float x = 0.f;
-                if (px < Xp) {
-                    int sx = px;
-                    if (!PREPADDED) {
-                        sx = px - H;
-                        if (sx < 0 || sx >= X) sx = reflect101(sx, X);
-                    }
-                    x = to_f32(srow[sx]);
-                }
-                v[i] = x;
-            }
+        for (int i = 0; i < NV; ++i) {
+            const int px = px0 + i;
+            float x = 0.f;
+            if (px < Xp) x = to_f32(srow[PREPADDED ? px : reflect101_near(px - H, X)]);
+            v[i] = x;
         }
-#pragma unroll
-        for (int i = 0; i < V::N; ++i) v[i] *= scale;
-    };
-    // two chunks per iteration, both loads issued before either store
+    }
+}
+
+// Resident blocks of 256 threads for a staging kernel instance: SMs x blocks per SM
+// (the occupancy is queried once per instance).
+template <auto Kernel>
+static unsigned stage_grid(long long groups) {
+    static const int per_sm = [] {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, Kernel, 256, 0) != cudaSuccess ||
+            n <= 0) {
+            cudaGetLastError();  // consume a non-sticky error; fall back to one block per SM
+            n = 1;
+        }
+        return n;
+    }();
+    const long long resident = (long long)device_sm_count() * per_sm;
+    return (unsigned)std::max<long long>(1, std::min(groups, resident));
+}
+
+// Plain layout [Zp][Yp][Xs]: rows of planes [pz0, pz0 + nplanes), kStageRows per warp.
+template <typename Tin, typename Tout, bool PREPADDED, bool VEC>
+__global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, int X, int Y,
+                                                    int Z, int H, int Hz, int Xp, int Yp, int pz0,
+                                                    int nplanes, int Xs, float scale,
+                                                    Tout* __restrict__ dst) {
+    using V = Vec16<Tout>;
+    const int lane = threadIdx.x & 31;
+    const int nrows = nplanes * Yp;
     const int nchunk = Xs / V::N;
-    int c = lane;
-    for (; c + 32 < nchunk; c += 64) {
-        float v0[V::N], v1[V::N];
-        chunk(c, v0);
-        chunk(c + 32, v1);
-        drow[c] = V::pack(v0);
-        drow[c + 32] = V::pack(v1);
+    const int wstep = gridDim.x * 8 * kStageRows;
+    int rb = (blockIdx.x * 8 + (threadIdx.x >> 5)) * kStageRows;
+    int py = rb % Yp, pz = pz0 + rb / Yp;  // of row rb
+    const int dpy = wstep % Yp, dpz = wstep / Yp;
+    for (; rb < nrows; rb += wstep) {
+        const Tin* srow[kStageRows];
+        typename V::T* drow[kStageRows];
+        bool live[kStageRows];
+#pragma unroll
+        for (int r = 0; r < kStageRows; ++r) {
+            live[r] = rb + r < nrows;
+            int ry = py + (live[r] ? r : 0), rz = pz;
+            while (ry >= Yp) {
+                ry -= Yp;
+                ++rz;
+            }
+            drow[r] = reinterpret_cast<typename V::T*>(dst + ((size_t)rz * Yp + ry) * Xs);
+            srow[r] = PREPADDED ? in + ((size_t)rz * Yp + ry) * Xp
+                                : in + ((size_t)reflect101_near(rz - Hz, Z) * Y +
+                                        reflect101_near(ry - H, Y)) * X;
+        }
+        for (int c0 = lane; c0 < nchunk; c0 += 32 * kStageSlots) {
+            float v[kStageRows][kStageSlots][V::N];
+#pragma unroll
+            for (int r = 0; r < kStageRows; ++r)
+#pragma unroll
+                for (int k = 0; k < kStageSlots; ++k)
+                    if (live[r] && c0 + 32 * k < nchunk)
+                        stage_chunk<Tin, V::N, PREPADDED, VEC>(srow[r], (c0 + 32 * k) * V::N, X, H,
+                                                              Xp, v[r][k]);
+#pragma unroll
+            for (int r = 0; r < kStageRows; ++r)
+#pragma unroll
+                for (int k = 0; k < kStageSlots; ++k)
+                    if (live[r] && c0 + 32 * k < nchunk) {
+#pragma unroll
+                        for (int i = 0; i < V::N; ++i) v[r][k][i] *= scale;
+                        drow[r][c0 + 32 * k] = V::pack(v[r][k]);
+                    }
+        }
+        py += dpy;
+        pz += dpz;
+        while (py >= Yp) {
+            py -= Yp;
+            ++pz;
+        }
     }
-    if (c < nchunk) {
-        float v0[V::N];
-        chunk(c, v0);
-        drow[c] = V::pack(v0);
+}
+
+// Row-pair layout: copy c, plane pz, pair k holds the padded rows 2k+c and 2k+c+1 as
+// half2.  A warp takes one (plane, pair k) per step and writes both copies' rows
+// from the three source rows 2k, 2k+1, 2k+2 (read once, instead of once per copy);
+// a 16-byte chunk is 4 columns.
+template <typename Tin, bool PREPADDED, bool VEC>
+__global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict__ in, int X, int Y,
+                                                          int Z, int H, int Xp, int Yp, int Xs,
+                                                          int Yq, size_t copy_elems, float scale,
+                                                          __half2* __restrict__ dst, int pz0,
+                                                          int nplanes) {
+    const int lane = threadIdx.x & 31;
+    const int npairs = nplanes * Yq;
+    const int nchunk = Xs / 4;
+    const int wstep = gridDim.x * 8;
+    int q = blockIdx.x * 8 + (threadIdx.x >> 5);
+    int k = q % Yq, pz = pz0 + q / Yq;
+    const int dk = wstep % Yq, dpz = wstep / Yq;
+    for (; q < npairs; q += wstep) {
+        const Tin* src[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const int row = 2 * k + e;
+            src[e] = nullptr;
+            if (row < Yp)
+                src[e] = PREPADDED ? in + ((size_t)pz * Yp + row) * Xp
+                                   : in + ((size_t)reflect101_near(pz - H, Z) * Y +
+                                           reflect101_near(row - H, Y)) * X;
+        }
+        uint4* drow0 = reinterpret_cast<uint4*>(dst + ((size_t)pz * Yq + k) * Xs);
+        uint4* drow1 = reinterpret_cast<uint4*>(dst + copy_elems + ((size_t)pz * Yq + k) * Xs);
+        for (int c0 = lane; c0 < nchunk; c0 += 32 * kStageSlots) {
+            float v[kStageSlots][3][4];
+#pragma unroll
+            for (int j = 0; j < kStageSlots; ++j)
+                if (c0 + 32 * j < nchunk) {
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) {
+                        if (src[e])
+                            stage_chunk<Tin, 4, PREPADDED, VEC>(src[e], (c0 + 32 * j) * 4, X, H, Xp,
+                                                                v[j][e]);
+                        else
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) v[j][e][i] = 0.f;
+                    }
+                }
+#pragma unroll
+            for (int j = 0; j < kStageSlots; ++j)
+                if (c0 + 32 * j < nchunk) {
+                    unsigned int w0[4], w1[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float a = v[j][0][i] * scale, b = v[j][1][i] * scale,
+                                    c = v[j][2][i] * scale;
+                        const __half2 e0 = __floats2half2_rn(a, b), e1 = __floats2half2_rn(b, c);
+                        w0[i] = *reinterpret_cast<const unsigned int*>(&e0);
+                        w1[i] = *reinterpret_cast<const unsigned int*>(&e1);
+                    }
+                    drow0[c0 + 32 * j] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+                    drow1[c0 + 32 * j] = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+                }
+        }
+        k += dk;
+        pz += dpz;
+        while (k >= Yq) {
+            k -= Yq;
+            ++pz;
+        }
     }
+}
+
+// Planes per launch so that a launch covers at most 2^30 rows: row indices, and a row
+// index plus a grid stride, stay within 32 bits.
+static int stage_planes_per_launch(long long rows_per_plane) {
+    return (int)std::max<long long>(1, (1LL << 30) / std::max<long long>(1, rows_per_plane));
+}
+
+template <typename Tin>
+static cudaError_t stage_pairs_typed(const void* in, bool prepadded, float scale, const Staging& st,
+                                     void* dst, cudaStream_t stream, int pz0, int pz1) {
+    const size_t copy_elems = st.copy_bytes() / 4;
+    const bool vec = reinterpret_cast<uintptr_t>(in) % (4 * sizeof(Tin)) == 0 &&
+                     (prepadded ? st.Xp % 4 == 0 : (st.X % 4 == 0 && st.H % 4 == 0));
+    const int step = stage_planes_per_launch(st.Yq);
+    for (int p0 = pz0; p0 < pz1; p0 += step) {
+        const int np = std::min(step, pz1 - p0);
+        const long long groups = ((long long)np * st.Yq + 7) / 8;
+#define GNLM_PAIRS_LAUNCH(P, VEC)                                                                  \
+    stage_pairs_kernel<Tin, P, VEC><<<stage_grid<stage_pairs_kernel<Tin, P, VEC>>(groups), 256, 0, \
+                                      stream>>>((const Tin*)in, st.X, st.Y, st.Z, st.H, st.Xp,      \
+                                                st.Yp, st.Xs, st.Yq, copy_elems, scale,             \
+                                                (__half2*)dst, p0, np)
+        if (prepadded) {
+            if (vec) GNLM_PAIRS_LAUNCH(true, true); else GNLM_PAIRS_LAUNCH(true, false);
+        } else {
+            if (vec) GNLM_PAIRS_LAUNCH(false, true); else GNLM_PAIRS_LAUNCH(false, false);
+        }
+#undef GNLM_PAIRS_LAUNCH
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 template <typename Tin, typename Tout>
 static cudaError_t stage_typed(const void* in, bool prepadded, float scale, const Staging& st,
                                void* dst, cudaStream_t stream, int pz0, int pz1) {
-    const long long row0 = (long long)st.Yp * pz0, row1 = (long long)st.Yp * pz1;
-    const unsigned blocks = (unsigned)((row1 - row0 + 7) / 8);
     constexpr int NV = Vec16<Tout>::N;
     const size_t vbytes = sizeof(Tin) * NV;
     const bool vec = reinterpret_cast<uintptr_t>(in) % vbytes == 0 &&
                      (prepadded ? st.Xp % NV == 0 : (st.X % NV == 0 && st.H % NV == 0));
-#define GNLM_STAGE_LAUNCH(P, VEC)                                                              \
-    stage_kernel<Tin, Tout, P, VEC><<<blocks, 256, 0, stream>>>(                                \
-        (const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz, st.Xp, st.Yp, row0, row1, st.Xs, scale, \
-        (Tout*)dst)
-    if (prepadded) {
-        if (vec) GNLM_STAGE_LAUNCH(true, true); else GNLM_STAGE_LAUNCH(true, false);
-    } else {
-        if (vec) GNLM_STAGE_LAUNCH(false, true); else GNLM_STAGE_LAUNCH(false, false);
-    }
+    const int step = stage_planes_per_launch(st.Yp);
+    for (int p0 = pz0; p0 < pz1; p0 += step) {
+        const int np = std::min(step, pz1 - p0);
+        const long long groups = ((long long)np * st.Yp + 8 * kStageRows - 1) / (8 * kStageRows);
+#define GNLM_STAGE_LAUNCH(P, VEC)                                                                   \
+    stage_kernel<Tin, Tout, P, VEC><<<stage_grid<stage_kernel<Tin, Tout, P, VEC>>(groups), 256, 0, \
+                                      stream>>>((const Tin*)in, st.X, st.Y, st.Z, st.H, st.Hz,      \
+                                                st.Xp, st.Yp, p0, np, st.Xs, scale, (Tout*)dst)
+        if (prepadded) {
+            if (vec) GNLM_STAGE_LAUNCH(true, true); else GNLM_STAGE_LAUNCH(true, false);
+        } else {
+            if (vec) GNLM_STAGE_LAUNCH(false, true); else GNLM_STAGE_LAUNCH(false, false);
+        }
 #undef GNLM_STAGE_LAUNCH
-    return cudaGetLastError();
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float scale,

@@ -165,6 +165,30 @@ def read_profile_traffic(kernel_key):
     return None
 
 
+def measured_hbm_peak():
+    """(GB/s, source) of the HBM copy peak: MEASURED_PEAKS.json at the repository root
+    (a STREAM-style copy measured on the GB300s), else the fallback figure."""
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            v = float(json.load(f)["hbm_gbs"])
+        if v > 0:
+            return v, "of measured (MEASURED_PEAKS.json hbm_gbs, copy)"
+    except (OSError, KeyError, ValueError, TypeError):
+        pass
+    return 6800.0, "of fallback (6.8 TB/s copy on a GB300)"
+
+
+def staging_bytes(shape, sr, pr, in_bytes=4, elem=4):
+    """Algorithmic bytes of one staging pass: the input read once and the padded
+    volume ([Z+2H][Y+2H][X+2H rounded up to 16 bytes]) written once."""
+    Z, Y, X = shape
+    H = sr + pr
+    per16 = 16 // elem
+    xs = (X + 2 * H + per16 - 1) // per16 * per16
+    return Z * Y * X * in_bytes + (Z + 2 * H) * (Y + 2 * H) * xs * elem
+
+
 def cpu_baseline(shape, budget_s=10.0):
     """Oracle FP32 separable form on a z-slab of the workload, all host threads."""
     import oracle as O
@@ -507,6 +531,9 @@ def run_gnlm(args):
     image2d = bench_2d(torch, gnlm) if not args.skip_extra else None
     large = bench_large_patch(torch, gnlm) if not args.skip_extra else None
     fused_mean = statistics.mean(fused_ms)
+    stage_mean = statistics.mean(stage_ms)
+    hbm_peak, hbm_src = measured_hbm_peak()
+    stage_gbs = staging_bytes(SHAPE, SR, PR) / (stage_mean * 1e-3) / 1e9
     achieved = FLOPS_PER_PAIR * OFFSETS * nvox / (fused_mean * 1e-3) / 1e12
     # FP32 variants 4-6 are the grouped-z kernel, 0-3 the one-offset-at-a-time kernel
     kname = "nlm3d_fwd_pz_kernel" if tuned32[0] >= 4 else "nlm3d_fwd_kernel"
@@ -530,10 +557,17 @@ def run_gnlm(args):
                      "peak_source": "FFMA probe kernel measured in this run (FP32 pipe; "
                                     "MEASURED_PEAKS.json has HBM and bf16 only)",
                      "algorithmic": f"{FLOPS_PER_PAIR} flops x {OFFSETS} offsets x {nvox} voxels"},
+        "staging_roofline": {"kernel": "stage_kernel<float,float> (REFLECT_101 pad + pre-scale)",
+                             "bound": "hbm", "achieved": round(stage_gbs, 1),
+                             "peak": round(hbm_peak, 1), "unit": "GB/s",
+                             "frac": round(stage_gbs / hbm_peak, 4), "peak_source": hbm_src,
+                             "traffic": read_profile_traffic("stage_kernel"),
+                             "algorithmic": "input read once + padded volume written once "
+                                            f"({staging_bytes(SHAPE, SR, PR)} bytes)"},
         "autotune": {"fp32": {"chosen": tuned32[0], "ms": [round(t, 4) for t in tuned32[1]]},
                      "fp16_storage": {"chosen": tuned16[0], "ms": [round(t, 4) for t in tuned16[1]]}},
         "fp32x2_probe_tflops": round(peak_x2, 3),
-        "kernels_ms": {"stage": round(statistics.mean(stage_ms), 4),
+        "kernels_ms": {"stage": round(stage_mean, 4),
                        "fused_fp32": round(fused_mean, 4),
                        "fused_fp16": round(statistics.mean(f16), 4)},
         "forms": {"fp32": {"value": round(value, 2), "max_abs_err_vs_fp64": err32,
