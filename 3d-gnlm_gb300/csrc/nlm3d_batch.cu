@@ -50,34 +50,65 @@ struct StageDesc {
     long long row0;  // first global padded row of this volume
 };
 
-// One block per padded row of any volume (row r of volume v: y = r % Yp, z = r / Yp).
+// Padded rows of every volume (row r of volume v: y = r % Yp, z = r / Yp), one warp
+// per row, resident blocks striding over the rows.  A warp finds its first row's
+// volume by binary search and then advances the volume index linearly (rows are
+// ordered by volume and a stride crosses few volumes), reloading the descriptor only
+// when the volume changes.  Each lane owns 16-byte output chunks (4 columns) c = lane
+// and lane + 32 of a row and issues both chunks' loads before either store; only the
+// 2H border columns reflect (reflect101_near, no division in the common case).
 __global__ void __launch_bounds__(256) batch_stage_kernel(const StageDesc* __restrict__ descs,
-                                                          int n) {
-    const long long row = blockIdx.x;
+                                                          int n, long long total_rows) {
+    const int lane = threadIdx.x & 31;
+    const long long wstep = (long long)gridDim.x * 8;
+    long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= total_rows) return;
     int lo = 0, hi = n - 1;
     while (lo < hi) {  // last volume whose row0 <= row
         const int mid = (lo + hi + 1) >> 1;
         if (descs[mid].row0 <= row) lo = mid; else hi = mid - 1;
     }
-    const StageDesc d = descs[lo];
-    const long long r = row - d.row0;
-    const int py = (int)(r % d.Yp), pz = (int)(r / d.Yp);
-    const int sy = reflect101(py - d.H, d.Y), sz = reflect101(pz - d.H, d.Z);
-    float* drow = static_cast<float*>(d.dst) + ((size_t)pz * d.Yp + py) * d.Xs;
-    const size_t src = ((size_t)sz * d.Y + sy) * d.X;
-    for (int px = threadIdx.x; px < d.Xs; px += blockDim.x) {
-        float v = 0.f;
-        if (px < d.Xp) {
-            const size_t i = src + reflect101(px - d.H, d.X);
+    StageDesc d = descs[lo];
+    long long next0 = lo + 1 < n ? descs[lo + 1].row0 : total_rows;
+    for (; row < total_rows; row += wstep) {
+        if (row >= next0) {
+            do {
+                ++lo;
+                next0 = lo + 1 < n ? descs[lo + 1].row0 : total_rows;
+            } while (row >= next0);
+            d = descs[lo];
+        }
+        const unsigned r = (unsigned)(row - d.row0);  // < Zp * Yp of one volume
+        const int py = (int)(r % (unsigned)d.Yp), pz = (int)(r / (unsigned)d.Yp);
+        const int sy = reflect101_near(py - d.H, d.Y), sz = reflect101_near(pz - d.H, d.Z);
+        float4* drow = reinterpret_cast<float4*>(static_cast<float*>(d.dst) +
+                                                 ((size_t)pz * d.Yp + py) * d.Xs);
+        const size_t src = ((size_t)sz * d.Y + sy) * d.X;
+        const int nchunk = d.Xs / 4;
+        auto load = [&](int px) -> float {
+            if (px >= d.Xp) return 0.f;
+            const size_t i = src + reflect101_near(px - d.H, d.X);
+            float v;
             if (d.in_dtype == NLM_U8)
                 v = (float)static_cast<const unsigned char*>(d.in)[i];
             else if (d.in_dtype == NLM_F16)
                 v = __half2float(static_cast<const __half*>(d.in)[i]);
             else
                 v = static_cast<const float*>(d.in)[i];
-            v *= d.scale;
+            return v * d.scale;
+        };
+        for (int c0 = lane; c0 < nchunk; c0 += 64) {
+            float v[2][4];
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                if (c0 + 32 * k < nchunk)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) v[k][i] = load(4 * (c0 + 32 * k) + i);
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                if (c0 + 32 * k < nchunk)
+                    drow[c0 + 32 * k] = make_float4(v[k][0], v[k][1], v[k][2], v[k][3]);
         }
-        drow[px] = v;
     }
 }
 
@@ -268,11 +299,21 @@ int prepare(nlm_batch_plan* p, int v) {
         cudaGraphExecDestroy(p->exec);
         p->exec = nullptr;
     }
+    // staging grid: resident blocks (SMs x blocks per SM), queried before the capture
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_stage_kernel, 256, 0) !=
+            cudaSuccess || per_sm <= 0) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const unsigned stage_blocks = (unsigned)std::max(
+        1LL, std::min((p->total_rows + 7) / 8, (long long)device_sm_count() * per_sm));
     cudaGraph_t graph = nullptr;
     e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->d_counter, 0, sizeof(int), p->cap_stream);
     if (e == cudaSuccess) {
-        batch_stage_kernel<<<(unsigned)p->total_rows, 256, 0, p->cap_stream>>>(p->d_stage, p->n);
+        batch_stage_kernel<<<stage_blocks, 256, 0, p->cap_stream>>>(p->d_stage, p->n,
+                                                                   p->total_rows);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = launch_variant(p, v, p->cap_stream, ctas, ew);

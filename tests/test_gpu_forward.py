@@ -97,6 +97,57 @@ def test_3d_prepadded_reference_layout(torch_cuda, gnlm_lib):
     assert np.abs(g - o).max() <= TOL_F32 * 255
 
 
+def _staging_scale(pr, h, dims=3):
+    """The pre-scale sqrt(log2(e) / (P h^2)) as the library computes it (double, then float)."""
+    P = float((2 * pr + 1) ** dims)
+    return np.float32(np.sqrt(1.4426950408889634 / (P * float(np.float32(h)) ** 2)))
+
+
+@pytest.mark.parametrize("shape", [(20, 24, 64), (9, 17, 45), (5, 6, 7)])
+@pytest.mark.parametrize("dt", [np.uint8, np.float16, np.float32])
+@pytest.mark.parametrize("fp16", [False, True])
+def test_3d_staging_layout_bit_exact(torch_cuda, gnlm_lib, shape, dt, fp16):
+    """The staging pass (REFLECT_101 on every axis, conversion, pre-scale) equals a numpy
+    construction of the same layout bit for bit: the plain [Zp][Yp][Xs] FP32 layout and
+    the FP16 row-pair copies E (rows 2k, 2k+1) and O (rows 2k+1, 2k+2), zero past the
+    last row and in the stride padding.  X = 64 takes the vector-load paths, X = 45 and
+    the 5 x 6 x 7 volume (halo as wide as the volume) the scalar ones."""
+    torch = torch_cuda
+    Z, Y, X = shape
+    sr, pr, h = 3, 1, 0.05
+    rng = np.random.default_rng(sum(shape))
+    if dt == np.uint8:
+        v = rng.integers(0, 256, shape, dtype=np.uint8)
+    else:
+        v = rng.random(shape).astype(dt)
+    x = torch.from_numpy(v).cuda()
+    nbytes = gnlm_lib.nlm3d_workspace_bytes(shape, sr, pr, fp16)
+    ws = torch.full((nbytes,), 0xAB, dtype=torch.uint8, device="cuda")
+    gnlm_lib.nlm3d_stage(x, sr, pr, h, ws, fp16_storage=fp16)
+    torch.cuda.synchronize()
+    host = ws.cpu().numpy()
+    H = sr + pr
+    pv = O.pad_reflect101(v.astype(np.float32), H) * _staging_scale(pr, h)  # float32 product
+    Zp, Yp, Xp = pv.shape
+    if not fp16:
+        Xs = (Xp + 3) // 4 * 4
+        st = host[:Zp * Yp * Xs * 4].view(np.float32).reshape(Zp, Yp, Xs)
+        assert np.array_equal(st[..., :Xp], pv)
+        assert not st[..., Xp:].any()
+    else:
+        Xs, Yq = (Xp + 3) // 4 * 4, (Yp + 2) // 2
+        copy_bytes = (Xs * Yq * Zp * 4 + 255) // 256 * 256
+        rows = np.zeros((Zp, 2 * Yq + 2, Xp), np.float16)
+        rows[:, :Yp] = pv.astype(np.float16)
+        for c in range(2):
+            cp = host[c * copy_bytes:c * copy_bytes + Xs * Yq * Zp * 4].view(np.float16)
+            cp = cp.reshape(Zp, Yq, Xs, 2)
+            for e in range(2):  # half e of pair k is padded row 2k + c + e
+                want = rows[:, c + e:c + e + 2 * Yq:2, :]
+                assert np.array_equal(cp[:, :, :Xp, e].view(np.uint16), want.view(np.uint16)), (c, e)
+            assert not cp[:, :, Xp:].view(np.uint16).any()
+
+
 def test_3d_host_path_and_workspace_forms_agree(torch_cuda, gnlm_lib):
     torch = torch_cuda
     v, _ = phantom.ellipsoid_phantom((20, 30, 50), sigma=0.05, seed=15)
