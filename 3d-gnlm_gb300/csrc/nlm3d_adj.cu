@@ -18,7 +18,7 @@
 // nlm3d_adj_kernel (gpad' over the padded domain + per-CTA h partial sums; the
 // tiles of a last, partial wave are split by offset runs over several CTAs whose
 // partial gpad' adj_tail_combine_kernel adds in part order),
-// adj_fold_kernel (REFLECT_101 fold, times s), adj_hgrad_kernel (ordered sum).
+// adj_fold_kernel (REFLECT_101 fold, times s), adj_hgrad_kernel (fixed-order sum).
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -375,7 +375,8 @@ __global__ void __launch_bounds__(32 * NW, 1)
     }
 }
 
-// gpad' of the tail tiles: the sum of their S partial bricks, in part order.
+// gpad' of the tail tiles: the sum of their S partial bricks, in part order.  Grid
+// (tail tiles, slices): the blocks of a tile split its voxels.
 template <int N, int RZ, int TY, int XO>
 __global__ void __launch_bounds__(256) adj_tail_combine_kernel(const AdjTail tl, int Xp, int Ypd,
                                                                int Zp, int Xs, int Yp,
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(256) adj_tail_combine_kernel(const AdjTail tl,
     constexpr int TILE_VOX = RZ * TY * 32;
     const int t = blockIdx.x, tile = tl.full + t;
     const int bx = tile % tl.nx, by = (tile / tl.nx) % tl.ny, bz = tile / (tl.nx * tl.ny);
-    for (int k = threadIdx.x; k < TILE_VOX; k += blockDim.x) {
+    for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < TILE_VOX; k += gridDim.y * blockDim.x) {
         const int lane = k & 31, row = (k >> 5) % TY, q = (k >> 5) / TY;
         const int px = bx * XO + lane - 2 * N, py = by * TY + row, pz = bz * RZ + q;
         if (lane < 2 * N || lane >= 32 - 2 * N || px >= Xp || py >= Ypd || pz >= Zp) continue;
@@ -399,13 +400,15 @@ __device__ __forceinline__ int preimages(int i, int n, int H, int* p) {
     int k = 0;
     p[k++] = i + H;
     for (int b = 0; b < H; ++b) {
-        if (reflect101(b - H, n) == i) p[k++] = b;
-        if (reflect101(n + b, n) == i) p[k++] = n + H + b;
+        if (reflect101_near(b - H, n) == i) p[k++] = b;
+        if (reflect101_near(n + b, n) == i) p[k++] = n + H + b;
     }
     return k;
 }
 
 // gin(x) = s * sum of gpad' over the padded positions that REFLECT_101 maps to x.
+// Columns H+1 .. X-2-H have the one preimage x + H (no border column reflects onto
+// them) and skip the preimage search; the summation order is the same either way.
 constexpr int kMaxHalo = 16;
 __global__ void __launch_bounds__(256) adj_fold_kernel(const float* __restrict__ gpad, int X,
                                                        int Y, int Z, int H, int Xs, int Yp,
@@ -415,25 +418,40 @@ __global__ void __launch_bounds__(256) adj_fold_kernel(const float* __restrict__
     const int nz = preimages(z, Z, H, pz);
     const int ny = preimages(y, Y, H, py);
     for (int x = threadIdx.x; x < X; x += blockDim.x) {
-        const int nx = preimages(x, X, H, px);
         float sum = 0.f;
-        for (int a = 0; a < nz; ++a)
-            for (int b = 0; b < ny; ++b) {
-                const float* row = gpad + ((size_t)pz[a] * Yp + py[b]) * Xs;
-                for (int c = 0; c < nx; ++c) sum += row[px[c]];
-            }
+        if (x > H && x < X - 1 - H) {
+            for (int a = 0; a < nz; ++a)
+                for (int b = 0; b < ny; ++b) sum += gpad[((size_t)pz[a] * Yp + py[b]) * Xs + x + H];
+        } else {
+            const int nx = preimages(x, X, H, px);
+            for (int a = 0; a < nz; ++a)
+                for (int b = 0; b < ny; ++b) {
+                    const float* row = gpad + ((size_t)pz[a] * Yp + py[b]) * Xs;
+                    for (int c = 0; c < nx; ++c) sum += row[px[c]];
+                }
+        }
         gin[((size_t)z * Y + y) * X + x] = s * sum;
     }
 }
 
-// dL/dh = -(2/h) * sum of the per-CTA partials, summed in index order by one thread.
-__global__ void adj_hgrad_kernel(const double* __restrict__ hpart, int n, double coef,
-                                 double* __restrict__ hgrad) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (int i = 0; i < n; ++i) s += hpart[i];
-        *hgrad = coef * s;
+// dL/dh = -(2/h) * sum of the per-CTA partials.  One block: thread t sums partials
+// t, t + 256, ... in index order, then a fixed binary tree adds the 256 thread sums.
+// The order never changes, so the result is bitwise reproducible.
+constexpr int kHgradThreads = 256;
+__global__ void __launch_bounds__(kHgradThreads) adj_hgrad_kernel(const double* __restrict__ hpart,
+                                                                  int n, double coef,
+                                                                  double* __restrict__ hgrad) {
+    __shared__ double red[kHgradThreads];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += kHgradThreads) s += hpart[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+#pragma unroll
+    for (int w = kHgradThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
     }
+    if (threadIdx.x == 0) *hgrad = coef * red[0];
 }
 
 // Tail split bounds: S * ntail <= min(SMs, kAdjMaxTailCtas), S <= kAdjMaxParts.
@@ -497,7 +515,8 @@ static cudaError_t run_adj3d(const Staging& st, const void* staged, const float*
                                                    gpad, hpart, tl, errword);
     if ((e = cudaGetLastError())) return e;
     if (tl.ntail > 0) {
-        adj_tail_combine_kernel<N, RZ, C::TY, C::XO><<<tl.ntail, 256, 0, stream>>>(
+        const dim3 cgrid(tl.ntail, (C::TILE_VOX + 255) / 256);
+        adj_tail_combine_kernel<N, RZ, C::TY, C::XO><<<cgrid, 256, 0, stream>>>(
             tl, st.Xp, st.Yp, st.Zp, st.Xs, st.Yp, gpad);
         if ((e = cudaGetLastError())) return e;
     }
@@ -506,7 +525,7 @@ static cudaError_t run_adj3d(const Staging& st, const void* staged, const float*
                                                   gin);
     if ((e = cudaGetLastError())) return e;
     if (hgrad) {
-        adj_hgrad_kernel<<<1, 32, 0, stream>>>(hpart, nblk, -2.0 / (double)h, hgrad);
+        adj_hgrad_kernel<<<1, kHgradThreads, 0, stream>>>(hpart, nblk, -2.0 / (double)h, hgrad);
         e = cudaGetLastError();
     }
     return e;
