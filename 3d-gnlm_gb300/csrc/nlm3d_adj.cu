@@ -59,16 +59,20 @@ struct Adj3d {
 };
 
 // (G, out') = (g / (s Z), s out) pairs, padded like the staged volume (zero outside).
+// One warp per padded row (8 rows per block, rows ordered (plane, row)).
 __global__ void __launch_bounds__(256) adj_aux_kernel(const float* __restrict__ g,
                                                       const float* __restrict__ out,
                                                       const float* __restrict__ zsum, int X,
                                                       int Y, int Z, int H, int Xs, int Yp,
-                                                      float s, float2* __restrict__ GO) {
-    const int py = blockIdx.x, pz = blockIdx.y;
+                                                      long long nrows, float s,
+                                                      float2* __restrict__ GO) {
+    const long long r = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= nrows) return;
+    const int py = (int)(r % Yp), pz = (int)(r / Yp);
     const int y = py - H, z = pz - H;
     const bool inside_yz = y >= 0 && y < Y && z >= 0 && z < Z;
     float2* row = GO + ((size_t)pz * Yp + py) * Xs;
-    for (int px = threadIdx.x; px < Xs; px += blockDim.x) {
+    for (int px = threadIdx.x & 31; px < Xs; px += 32) {
         const int x = px - H;
         float2 go = make_float2(0.f, 0.f);
         if (inside_yz && x >= 0 && x < X) {
@@ -488,9 +492,9 @@ static cudaError_t run_adj3d(const Staging& st, const void* staged, const float*
                              double* hpart, float* side, unsigned int* errword,
                              cudaStream_t stream) {
     using C = Adj3d<M, N, RY, RZ, NW>;
-    dim3 rows(st.Yp, st.Zp);
-    adj_aux_kernel<<<rows, 256, 0, stream>>>(d_gout, d_out, d_zsum, st.X, st.Y, st.Z, st.H, st.Xs,
-                                              st.Yp, s, GO);
+    const long long nrows = (long long)st.Yp * st.Zp;
+    adj_aux_kernel<<<(unsigned)((nrows + 7) / 8), 256, 0, stream>>>(
+        d_gout, d_out, d_zsum, st.X, st.Y, st.Z, st.H, st.Xs, st.Yp, nrows, s, GO);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     CUtensorMap vmap, gomap;

@@ -326,9 +326,11 @@ def bench_large_patch(torch, gnlm, reps=3):
 def bench_adjoint(torch, gnlm, peak_tflops, steps=50, reps=20):
     """128^3 (ellipsoids, sigma 0.05, sr 3, pr 1): forward + adjoint per step (median
     of `reps` device-timed pairs), then used to fit h by gradient descent on the MSE
-    to the clean phantom."""
+    to the clean phantom.  The forward's tile shape is autotuned on this volume first
+    (the project's autotuner, as for the 2D and large-patch workloads)."""
     from gnlm import phantom
     noisy, clean = phantom.ellipsoid_phantom((128, 128, 128), n_ellipsoids=16, sigma=0.05, seed=4)
+    fwd_variant, _ = gnlm.autotune(3, (128, 128, 128), SR, PR)
     x, c = torch.from_numpy(noisy).cuda(), torch.from_numpy(clean).cuda()
     n = x.numel()
     ws = torch.empty(gnlm.lib().nlm3d_adjoint_workspace_bytes(128, 128, 128, SR, PR),
@@ -379,6 +381,7 @@ def bench_adjoint(torch, gnlm, peak_tflops, steps=50, reps=20):
     return {"shape": [128, 128, 128], "search_radius": SR, "patch_radius": PR,
             "fwd_ms": round(fwd_ms, 3), "adjoint_ms": round(adj_ms, 3),
             "fwd_adjoint_ms_per_step": round(fwd_ms + adj_ms, 3), "timing": f"median of {reps}",
+            "fwd_variant": fwd_variant,
             "adjoint_tflops": round(adj_tflops, 3),
             "adjoint_frac_fp32_peak": round(adj_tflops / peak_tflops, 4) if peak_tflops else None,
             "adjoint_algorithmic": f"{ADJ_FLOPS_PER_PAIR} flops x {OFFSETS} offsets x {padded} "

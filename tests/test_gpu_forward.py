@@ -280,6 +280,30 @@ def test_autotune_records_a_variant(torch_cuda, gnlm_lib):
     assert gnlm_lib.get_variant(3, 3, 1) == 6
 
 
+def test_3d_default_tile_shape_follows_the_volume(torch_cuda, gnlm_lib):
+    """With no recorded variant, a patch-3 volume that 4 x 8 tiles would cover in fewer
+    than ten waves runs on the 4 x 6 tiles (variant 5); 256^3 keeps the 4 x 8 tiles.
+    The two shapes slide their z windows from different planes, so their bits differ
+    and the default's output shows which one ran."""
+    torch = torch_cuda
+    try:
+        for shape, expect in [((64, 64, 64), 5), ((256, 256, 256), 6)]:
+            v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=8, sigma=0.05, seed=31)
+            x = torch.from_numpy(v).cuda()
+            outs = {}
+            for var in (5, 6):
+                gnlm_lib.set_variant(3, 3, 1, var)
+                outs[var] = gnlm_lib.nlm3d_forward(x, 3, 1, 0.05).cpu().numpy()
+            gnlm_lib.set_variant(3, 3, 1, -1)
+            d = gnlm_lib.nlm3d_forward(x, 3, 1, 0.05).cpu().numpy()
+            assert np.array_equal(d, outs[expect]), shape
+            if not np.array_equal(outs[5], outs[6]):
+                assert not np.array_equal(d, outs[11 - expect]), shape
+            assert np.abs(outs[5] - outs[6]).max() <= TOL_F32
+    finally:
+        gnlm_lib.set_variant(3, 3, 1, -1)
+
+
 @pytest.mark.parametrize("fp16", [False, True])
 def test_2d_every_tile_variant(torch_cuda, gnlm_lib, fp16):
     tol = TOL_F16 if fp16 else TOL_F32
