@@ -156,6 +156,11 @@ __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, 
     const int lane = threadIdx.x & 31;
     const int nrows = nplanes * Yp;
     const int nchunk = Xs / V::N;
+    // Lane order rotated by the chunks past the source row's end: index i holds chunk
+    // (i - rot) mod nchunk, so the right and left border chunks (the scalar reflect
+    // path) fall in the first slot of neighbouring lanes and a row diverges once.
+    const int rot = PREPADDED ? 0 : nchunk - min(nchunk, (X + H) / V::N);
+    auto chunk_of = [&](int i) { return i < rot ? i + nchunk - rot : i - rot; };
     const int wstep = gridDim.x * 8 * kStageRows;
     int rb = (blockIdx.x * 8 + (threadIdx.x >> 5)) * kStageRows;
     int py = rb % Yp, pz = pz0 + rb / Yp;  // of row rb
@@ -184,8 +189,8 @@ __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, 
 #pragma unroll
                 for (int k = 0; k < kStageSlots; ++k)
                     if (live[r] && c0 + 32 * k < nchunk)
-                        stage_chunk<Tin, V::N, PREPADDED, VEC>(srow[r], (c0 + 32 * k) * V::N, X, H,
-                                                              Xp, v[r][k]);
+                        stage_chunk<Tin, V::N, PREPADDED, VEC>(
+                            srow[r], chunk_of(c0 + 32 * k) * V::N, X, H, Xp, v[r][k]);
 #pragma unroll
             for (int r = 0; r < kStageRows; ++r)
 #pragma unroll
@@ -193,7 +198,7 @@ __global__ void __launch_bounds__(256) stage_kernel(const Tin* __restrict__ in, 
                     if (live[r] && c0 + 32 * k < nchunk) {
 #pragma unroll
                         for (int i = 0; i < V::N; ++i) v[r][k][i] *= scale;
-                        drow[r][c0 + 32 * k] = V::pack(v[r][k]);
+                        drow[r][chunk_of(c0 + 32 * k)] = V::pack(v[r][k]);
                     }
         }
         py += dpy;
@@ -218,6 +223,9 @@ __global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict_
     const int lane = threadIdx.x & 31;
     const int npairs = nplanes * Yq;
     const int nchunk = Xs / 4;
+    // border chunks in the first slot of neighbouring lanes (as in stage_kernel)
+    const int rot = PREPADDED ? 0 : nchunk - min(nchunk, (X + H) / 4);
+    auto chunk_of = [&](int i) { return i < rot ? i + nchunk - rot : i - rot; };
     const int wstep = gridDim.x * 8;
     int q = blockIdx.x * 8 + (threadIdx.x >> 5);
     int k = q % Yq, pz = pz0 + q / Yq;
@@ -243,8 +251,8 @@ __global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict_
 #pragma unroll
                     for (int e = 0; e < 3; ++e) {
                         if (src[e])
-                            stage_chunk<Tin, 4, PREPADDED, VEC>(src[e], (c0 + 32 * j) * 4, X, H, Xp,
-                                                                v[j][e]);
+                            stage_chunk<Tin, 4, PREPADDED, VEC>(src[e], chunk_of(c0 + 32 * j) * 4, X,
+                                                                H, Xp, v[j][e]);
                         else
 #pragma unroll
                             for (int i = 0; i < 4; ++i) v[j][e][i] = 0.f;
@@ -262,8 +270,8 @@ __global__ void __launch_bounds__(256) stage_pairs_kernel(const Tin* __restrict_
                         w0[i] = *reinterpret_cast<const unsigned int*>(&e0);
                         w1[i] = *reinterpret_cast<const unsigned int*>(&e1);
                     }
-                    drow0[c0 + 32 * j] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-                    drow1[c0 + 32 * j] = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+                    drow0[chunk_of(c0 + 32 * j)] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+                    drow1[chunk_of(c0 + 32 * j)] = make_uint4(w1[0], w1[1], w1[2], w1[3]);
                 }
         }
         k += dk;
