@@ -99,8 +99,9 @@ __device__ __forceinline__ void load_vec(const Tin* p, float* v) {
     }
 }
 
-// Staging kernels, both layouts.  A warp copies whole padded rows: each lane owns
-// 16-byte output chunks c = lane, lane + 32, ... of a row and issues the loads of all
+// Staging kernels, both layouts.  A warp copies whole padded rows: each lane owns the
+// 16-byte output chunks at indices lane, lane + 32, ... of a row (the chunk order is
+// rotated, see `rot` in the kernels) and issues the loads of all
 // its chunks of kStageRows rows (kStageSlots per row and pass) before the first
 // store, so a warp keeps about 2 KB in flight.  Blocks stay resident (grid = SMs x
 // blocks per SM) and stride over row groups; a thread divides once, at the start,
