@@ -193,7 +193,7 @@ struct nlm_batch_plan {
 
 namespace {
 
-constexpr int kBatchVariants = 3;  // (RY, RZ): (4, 8), (4, 4), (2, 8); 4 warps
+constexpr int kBatchVariants = NLM_BATCH_VARIANTS;  // (RY, RZ): (4, 8), (4, 4), (2, 8), (4, 6); 4 warps
 
 // Sets the kernel's shared-memory limit and returns its persistent grid size.
 template <int RY, int RZ, int MINB>
@@ -221,6 +221,7 @@ cudaError_t config_variant(nlm_batch_plan* p, int v, int* ctas) {
         case 0: return config_batch<4, 8, 2>(p, ctas);
         case 1: return config_batch<4, 4, 2>(p, ctas);
         case 2: return config_batch<2, 8, 2>(p, ctas);
+        case 3: return config_batch<4, 6, 2>(p, ctas);
     }
     return cudaErrorInvalidValue;
 }
@@ -230,12 +231,13 @@ cudaError_t launch_variant(nlm_batch_plan* p, int v, cudaStream_t s, int ctas, u
         case 0: return launch_batch<4, 8, 2>(p, s, ctas, ew);
         case 1: return launch_batch<4, 4, 2>(p, s, ctas, ew);
         case 2: return launch_batch<2, 8, 2>(p, s, ctas, ew);
+        case 3: return launch_batch<4, 6, 2>(p, s, ctas, ew);
     }
     return cudaErrorInvalidValue;
 }
 
 int tile_ty(int v) { return v == 2 ? 8 : 16; }  // NW (4) x RY
-int tile_rz(int v) { return v == 1 ? 4 : 8; }
+int tile_rz(int v) { return v == 1 ? 4 : v == 3 ? 6 : 8; }
 
 // Work list for tile shape v: all tiles of all volumes, most expensive first.
 void build_items(nlm_batch_plan* p, int v) {

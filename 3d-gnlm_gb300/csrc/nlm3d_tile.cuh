@@ -255,6 +255,16 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
     return true;
 }
 
+// Window row of element e of row pair p in the grouped kernel's packed arithmetic.
+// With patch radius 1 the two halo rows (0 and RY + 1) form pair 0 and pairs 1..RY/2
+// are rows (2p - 1, 2p): the centre rows of output rows (2k, 2k + 1) are then the
+// aligned pair k + 1, and the candidate centre values enter the packed weighted-sum
+// FMA without register moves.  Other radii pair rows (2p, 2p + 1).
+template <int N, int RY>
+__host__ __device__ constexpr int pz_row(int p, int e) {
+    return N == 1 ? (p == 0 ? (e == 0 ? 0 : RY + 1) : 2 * p - 1 + e) : 2 * p + e;
+}
+
 // Grouped z offsets (FP32, reference values in registers): the GZ offsets
 // (ox, oy, oz+g), g < GZ, share every candidate plane.  With c(j) the candidate plane
 // j of offset oz's stream, offset oz+g's difference at the thread's plane pl is
@@ -308,8 +318,8 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
     for (int pl = 0; pl < C::PLANES; ++pl)
 #pragma unroll
         for (int rp = 0; rp < RP; ++rp)
-            areg[pl][rp] = make_float2(aptr[pl * C::PLANE + (2 * rp) * C::BX],
-                                       aptr[pl * C::PLANE + (2 * rp + 1) * C::BX]);
+            areg[pl][rp] = make_float2(aptr[pl * C::PLANE + pz_row<N, RY>(rp, 0) * C::BX],
+                                       aptr[pl * C::PLANE + pz_row<N, RY>(rp, 1) * C::BX]);
 
     float2 zacc[OP][RZ], nacc[OP][RZ];
 #pragma unroll
@@ -319,13 +329,13 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
     const float2 minus1 = make_float2(-1.f, -1.f);
 
     // y box, x box, weight and accumulation of output plane q from the z-window sums S
-    // of rows 0..ROWS-1, with candidate centres cc (rows N..N+RY-1).
-    auto emit = [&](const float2 (&S)[RP], const int q, const float (&cc)[RY]) {
+    // of the row pairs, with candidate centres cc (output rows 2op, 2op + 1 in cc[op]).
+    auto emit = [&](const float2 (&S)[RP], const int q, const float2 (&cc)[OP]) {
         float Srow[C::ROWS];
 #pragma unroll
         for (int rp = 0; rp < RP; ++rp) {
-            Srow[2 * rp] = S[rp].x;
-            Srow[2 * rp + 1] = S[rp].y;
+            Srow[pz_row<N, RY>(rp, 0)] = S[rp].x;
+            Srow[pz_row<N, RY>(rp, 1)] = S[rp].y;
         }
         float Yv[RY];
         if constexpr (N == 1) {
@@ -360,7 +370,7 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
             }
             const float2 w = make_float2(ex2_neg(xv.x), ex2_neg(xv.y));
             zacc[op][q] = __fadd2_rn(zacc[op][q], w);
-            nacc[op][q] = __ffma2_rn(w, make_float2(cc[2 * op], cc[2 * op + 1]), nacc[op][q]);
+            nacc[op][q] = __ffma2_rn(w, cc[op], nacc[op][q]);
         }
     };
 
@@ -369,18 +379,28 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
         constexpr int JEND = C::PLANES + G - 1;
         float2 S[G][RP];
         float2 tr[G][C::K][RP];
-        float cand[N + 1][RY];
+        float2 cand[N + 1][OP];  // candidate centres of the last N + 1 planes, output row pairs
 #pragma unroll
         for (int j = 0; j < JEND; ++j) {
             float2 c2[RP];
 #pragma unroll
             for (int rp = 0; rp < RP; ++rp) {
-                const float b0 = bptr[j * C::PLANE + (2 * rp) * C::BX];
-                const float b1 = bptr[j * C::PLANE + (2 * rp + 1) * C::BX];
+                const float b0 = bptr[j * C::PLANE + pz_row<N, RY>(rp, 0) * C::BX];
+                const float b1 = bptr[j * C::PLANE + pz_row<N, RY>(rp, 1) * C::BX];
                 c2[rp] = make_float2(b0, b1);
-                const int r0 = 2 * rp, r1 = 2 * rp + 1;
-                if (r0 >= N && r0 < RY + N) cand[j % (N + 1)][r0 - N] = b0;
-                if (r1 >= N && r1 < RY + N) cand[j % (N + 1)][r1 - N] = b1;
+                if constexpr (N == 1) {
+                    if (rp >= 1) cand[j % 2][rp - 1] = c2[rp];  // rows (2rp - 1, 2rp)
+                } else {
+                    const int r0 = pz_row<N, RY>(rp, 0), r1 = pz_row<N, RY>(rp, 1);
+                    if (r0 >= N && r0 < RY + N) {
+                        if ((r0 - N) & 1) cand[j % (N + 1)][(r0 - N) / 2].y = b0;
+                        else cand[j % (N + 1)][(r0 - N) / 2].x = b0;
+                    }
+                    if (r1 >= N && r1 < RY + N) {
+                        if ((r1 - N) & 1) cand[j % (N + 1)][(r1 - N) / 2].y = b1;
+                        else cand[j % (N + 1)][(r1 - N) / 2].x = b1;
+                    }
+                }
             }
 #pragma unroll
             for (int g = 0; g < G; ++g) {

@@ -158,14 +158,14 @@ int check_dims3(int X, int Y, int Z, int H) {
 int report_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
 // Variant used before any autotuning: the fastest measured on a GB300 for the
-// configuration family (3D FP32 patch 3: z offsets in groups of three, 4 x 8;
-// search 11 / patch 5: groups of three, 4 x 6; 2D FP32: two columns per lane, 8 rows
-// x 4 warps), else variant 0.
+// configuration family (3D FP32 patch 3: z offsets in groups of three, 4 x 6 tiles,
+// faster than 4 x 8 from 64^3 to 256^3; search 11 / patch 5: groups of three, 4 x 6;
+// 2D FP32: two columns per lane, 8 rows x 4 warps), else variant 0.
 int default_variant(int dims, int sr, int pr, bool fp16) {
     if (fp16) return 0;
     if (dims == 3) {
         if (nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
-        if (pr == 1) return 6;
+        if (pr == 1) return 5;
         if (pr == 2 && sr == 5) return 5;
         return 0;
     }
@@ -176,26 +176,6 @@ int tuned_variant(int dims, int sr, int pr, bool fp16) {
     std::lock_guard<std::mutex> lk(g_mutex);
     auto it = g_tuned.find(tune_key(dims, sr, pr, fp16));
     return it == g_tuned.end() ? default_variant(dims, sr, pr, fp16) : it->second;
-}
-
-// The variant a 3D forward over an X x Y x Z volume uses: the recorded one, else the
-// default, except that with patch radius 1 a volume that the 4 x 8 tiles (variant 6,
-// 30 x 16 x 8 outputs per CTA, two CTAs per SM) would cover in fewer than ten waves
-// takes the 4 x 6 tiles (variant 5) instead: their grid fills the SMs better.
-// Measured on a GB300 (sr 3, ms, variant 5 vs 6): 64^3 0.089 vs 0.112, 128^3 0.415
-// vs 0.449, 192^3 1.215 vs 1.221, 256^3 2.750 vs 2.688.
-int tuned_variant3d(int sr, int pr, bool fp16, int X, int Y, int Z) {
-    {
-        std::lock_guard<std::mutex> lk(g_mutex);
-        auto it = g_tuned.find(tune_key(3, sr, pr, fp16));
-        if (it != g_tuned.end()) return it->second;
-    }
-    const int v = default_variant(3, sr, pr, fp16);
-    if (v == 6) {
-        const long long ctas = (long long)((X + 29) / 30) * ((Y + 15) / 16) * ((Z + 7) / 8);
-        if (ctas < 10LL * 2 * device_sm_count()) return 5;
-    }
-    return v;
 }
 
 unsigned int* device_error_word() {
@@ -330,7 +310,7 @@ static int fwd3d_staged_impl(const void* d_ws, int X, int Y, int Z, int sr, int 
     const int H = sr + pr;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
     Staging st = staging3d(X, Y, Z, H, fp16);
-    cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, tuned_variant3d(sr, pr, fp16, X, Y, Z),
+    cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, tuned_variant(3, sr, pr, fp16),
                                      1.0f / weight_scale(pr, 3, h), d_out, d_zsum,
                                      device_error_word(), stream);
     if (e != cudaSuccess) return cuda_fail(e, "nlm3d_fwd launch");
@@ -556,7 +536,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
     const bool prepadded = (flags & NLM_FLAG_PREPADDED) != 0;
     const int H = sr + pr;
-    const int variant = tuned_variant3d(sr, pr, fp16, X, Y, Z);
+    const int variant = tuned_variant(3, sr, pr, fp16);
     const int RZ = nlm3d_fwd_tile_z(sr, pr, fp16, variant);
     if (RZ <= 0) return 1;
     const int CZ = std::max(1, (Z / 16 + RZ - 1) / RZ) * RZ;

@@ -92,9 +92,6 @@ int device_sm_count();
 // Tile-shape variant the forward uses for (dims, sr, pr, fp16): the autotuned
 // choice if one was recorded, else default_variant().
 int tuned_variant(int dims, int sr, int pr, bool fp16);
-// The variant of a 3D forward over an X x Y x Z volume (recorded, else a default that
-// depends on the volume for patch radius 1).
-int tuned_variant3d(int sr, int pr, bool fp16, int X, int Y, int Z);
 int default_variant(int dims, int sr, int pr, bool fp16);
 
 // 2D forward over a staged image (Z = 1, Hz = 0).

@@ -233,7 +233,7 @@ class BatchPlan:
     ``volumes`` is a list of (tensor [Z, Y, X], sr, pr, h); outputs are allocated here.
     """
 
-    N_VARIANTS = 3
+    N_VARIANTS = 4
 
     def __init__(self, volumes, with_zsum=False):
         torch = _torch()

@@ -187,9 +187,10 @@ typedef struct nlm_batch_plan nlm_batch_plan;
  * expensive first) and captures a CUDA graph [reset work counter -> stage all
  * volumes -> persistent NLM kernel].  nlm3d_batch_run replays the graph on
  * `stream` (asynchronous).  nlm3d_batch_autotune times each tile shape on the
- * batch, keeps the fastest, and returns its index (times_ms: one entry per shape,
- * nullable).  flags must be 0 (FP32).
+ * batch, keeps the fastest, and returns its index (times_ms: NLM_BATCH_VARIANTS
+ * entries, one per shape, nullable).  flags must be 0 (FP32).
  */
+#define NLM_BATCH_VARIANTS 4
 int nlm3d_batch_create(const nlm_volume* vols, int n, unsigned int flags, nlm_batch_plan** plan);
 int nlm3d_batch_run(nlm_batch_plan* plan, nlm_stream_t stream);
 int nlm3d_batch_autotune(nlm_batch_plan* plan, float* times_ms, nlm_stream_t stream);
@@ -208,10 +209,7 @@ int nlm3d_forward_batched(const nlm_volume* vols, int n, nlm_stream_t stream);
  * whose block/grid shape is fixed by macros, 3DNLM/main.cu:15-21).  Forward calls
  * use the recorded variant for (dims, sr, pr, FP16 flag), or, when none is
  * recorded (or after a reset with -1), a per-configuration default measured on a
- * GB300; nlm_get_variant reports whichever applies.  One default depends on the
- * volume: a 3D FP32 forward with patch radius 1 that the default 4 x 8 tiles would
- * cover in fewer than ten waves of CTAs (two per SM) uses the 4 x 6 tiles (variant 5)
- * instead; nlm_get_variant, which has no volume, reports the 4 x 8 default.
+ * GB300; nlm_get_variant reports whichever applies.
  */
 int nlm_variant_count(int dims, unsigned int flags);
 int nlm_set_variant(int dims, int sr, int pr, unsigned int flags, int variant); /* -1 = reset */
