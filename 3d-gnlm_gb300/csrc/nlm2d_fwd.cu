@@ -72,17 +72,12 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         fence_mbar_init();
     }
     __syncthreads();
+    const bool skip = inject_skip_copy(errword, blockIdx.x, blockIdx.y, 0);  // test builds only
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(bar, C::TILE_BYTES);
-        tma_load_2d(tile, &tmap, xs, Y0, bar);
+        if (!skip) tma_load_2d(tile, &tmap, xs, Y0, bar);
     }
-    if (!mbar_wait_bounded(bar, 0)) {
-        if (threadIdx.x == 0) {
-            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
-            mbar_wait_bounded(bar, 0);
-        }
-        return;
-    }
+    if (!tile_copy_wait(bar, 0, errword, skip)) return;
 
     const T* aptr = tile + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
     if constexpr (kBoundsCheck) {  // offsets +-M around ROWS rows (groups reach the same rows)
@@ -310,17 +305,12 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         fence_mbar_init();
     }
     __syncthreads();
+    const bool skip = inject_skip_copy(errword, blockIdx.x, blockIdx.y, 0);  // test builds only
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(bar, C::TILE_FLOATS * 4);
-        tma_load_2d(tile, &tmap, xs, Y0, bar);
+        if (!skip) tma_load_2d(tile, &tmap, xs, Y0, bar);
     }
-    if (!mbar_wait_bounded(bar, 0)) {
-        if (threadIdx.x == 0) {
-            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
-            mbar_wait_bounded(bar, 0);
-        }
-        return;
-    }
+    if (!tile_copy_wait(bar, 0, errword, skip)) return;
     for (int i = threadIdx.x; i < C::TILE_FLOATS - 1; i += 32 * NW) shifted[i] = tile[i + 1];
     __syncthreads();
 

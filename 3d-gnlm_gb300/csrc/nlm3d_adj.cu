@@ -167,18 +167,15 @@ __global__ void __launch_bounds__(32 * NW, 1)
         fence_mbar_init();
     }
     __syncthreads();
+    const bool skip = inject_skip_copy(errword, bx, by, bz);  // test builds only
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(bar, C::FIELD_BYTES + C::GO_BYTES);
-        tma_load_3d(vt, &vmap, org_x, org_y, org_z, bar);
-        tma_load_3d(got, &gomap, 2 * org_x, org_y, org_z, bar);
-    }
-    if (!mbar_wait_bounded(bar, 0)) {
-        if (threadIdx.x == 0) {
-            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
-            mbar_wait_bounded(bar, 0);
+        if (!skip) {
+            tma_load_3d(vt, &vmap, org_x, org_y, org_z, bar);
+            tma_load_3d(got, &gomap, 2 * org_x, org_y, org_z, bar);
         }
-        return;
     }
+    if (!tile_copy_wait(bar, 0, errword, skip)) return;
 
     // smem position of this thread's (row 0, plane 0) output voxel
     int sx = lane + C::HE + ral;

@@ -97,18 +97,13 @@ __device__ __forceinline__ bool fwd3d_tile(const CUtensorMap* map, T* tile, uint
     const int xs = X0 & ~(C::A - 1);  // 16-byte aligned TMA start column
     const int ral = X0 - xs;
 
+    const bool skip = inject_skip_copy(errword, bx, by, bz);  // false outside test builds
     if (threadIdx.x == 0) {
         fence_proxy_async_smem();  // earlier generic reads of the tile before the async write
         mbar_arrive_expect_tx(bar, C::TILE_BYTES);
-        tma_load_3d(tile, map, xs, Y0, Z0, bar);
+        if (!skip) tma_load_3d(tile, map, xs, Y0, Z0, bar);
     }
-    if (!mbar_wait_bounded(bar, parity)) {
-        if (threadIdx.x == 0) {
-            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
-            mbar_wait_bounded(bar, parity);  // give an in-flight copy a last chance to land
-        }
-        return false;
-    }
+    if (!tile_copy_wait(bar, parity, errword, skip)) return false;
 
     // Reference values: lane's column, rows warp*RY + H - N + rr, planes H - N + pl.
     const T* aptr = tile + (C::H - N) * C::PLANE + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
@@ -291,18 +286,13 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
     const int xs = X0 & ~(C::A - 1);
     const int ral = X0 - xs;
 
+    const bool skip = inject_skip_copy(errword, bx, by, bz);  // false outside test builds
     if (threadIdx.x == 0) {
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(bar, C::TILE_BYTES);
-        tma_load_3d(tile, map, xs, Y0, Z0, bar);
+        if (!skip) tma_load_3d(tile, map, xs, Y0, Z0, bar);
     }
-    if (!mbar_wait_bounded(bar, parity)) {
-        if (threadIdx.x == 0) {
-            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
-            mbar_wait_bounded(bar, parity);
-        }
-        return false;
-    }
+    if (!tile_copy_wait(bar, parity, errword, skip)) return false;
 
     const float* aptr =
         tile + (C::H - N) * C::PLANE + (warp * RY + C::H - N) * C::BX + (lane + M + ral);
@@ -520,20 +510,17 @@ __device__ __forceinline__ bool fwd3d_tile_h2(const CUtensorMap* mapE, const CUt
     const __half2* E = reinterpret_cast<const __half2*>(smem);
     const __half2* O = reinterpret_cast<const __half2*>(smem + C::COPY_STRIDE);
 
+    const bool skip = inject_skip_copy(errword, bx, by, bz);  // false outside test builds
     if (threadIdx.x == 0) {
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(bar, 2 * C::COPY_BYTES);
         // E pair k = rows (2k, 2k+1) from pair Y0/2; O pair k = rows (2k+1, 2k+2) from Y0/2 - 1
-        tma_load_3d(smem, mapE, xs, Y0 / 2, Z0, bar);
-        tma_load_3d(smem + C::COPY_STRIDE, mapO, xs, Y0 / 2 - 1, Z0, bar);
-    }
-    if (!mbar_wait_bounded(bar, parity)) {
-        if (threadIdx.x == 0) {
-            raise_device_error(errword, DEVERR_TMA_TIMEOUT);
-            mbar_wait_bounded(bar, parity);
+        if (!skip) {
+            tma_load_3d(smem, mapE, xs, Y0 / 2, Z0, bar);
+            tma_load_3d(smem + C::COPY_STRIDE, mapO, xs, Y0 / 2 - 1, Z0, bar);
         }
-        return false;
     }
+    if (!tile_copy_wait(bar, parity, errword, skip)) return false;
 
     // Row pair (r, r+1) of the tile, r = Y0 + j: in E at index j/2 if r is even, in O at
     // (j+1)/2 if odd.  The thread's rows start at j = warp*RY + M (+ oy for candidates).

@@ -17,9 +17,10 @@
 
 namespace gnlm {
 
-// One error word per device; kernels OR DEVERR_* bits into it when a bounded
-// wait gives up (see nlm_device_status).
-__device__ unsigned int g_device_error_word;
+// Per device: [0] the error word, which kernels OR DEVERR_* bits into when a bounded
+// wait gives up (see nlm_device_status); [1] the fault-injection control word that
+// only the NLM_BOUNDS_CHECK test build reads (see nlm_test_set_fault).
+__device__ unsigned int g_device_error_word[2];
 
 namespace {
 
@@ -43,7 +44,6 @@ int cuda_fail(cudaError_t e, const char* what) {
 }
 
 std::mutex g_mutex;
-std::map<int, unsigned int*> g_errword;                    // device -> error word address
 std::map<std::pair<int, cudaStream_t>, std::pair<void*, size_t>> g_ws;  // cached workspaces
 
 struct HostPath {
@@ -157,6 +157,74 @@ int check_dims3(int X, int Y, int Z, int H) {
 
 int report_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
+int validate_forward3d(const void* in, const void* out, int in_dtype, int X, int Y, int Z, int sr,
+                       int pr, float h, unsigned int flags) {
+    int rc = check_common(in, out, in_dtype, sr, pr, h, flags);
+    if (rc) return rc;
+    if ((rc = check_dims3(X, Y, Z, sr + pr))) return rc;
+    if (!nlm3d_fwd_supported(sr, pr, (flags & NLM_FLAG_FP16_STORAGE) != 0))
+        return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
+    return NLM_OK;
+}
+
+namespace {
+using PFN_ctxGetCurrent = CUresult (*)(CUcontext*);
+using PFN_ctxGetId = CUresult (*)(CUcontext, unsigned long long*);
+PFN_ctxGetCurrent g_ctx_current = nullptr;
+PFN_ctxGetId g_ctx_id = nullptr;
+std::map<std::pair<unsigned long long, const void*>, void*> g_symbols;  // (context, symbol)
+
+}  // namespace
+
+// Unique ID of the calling thread's current context (false if there is none yet).
+bool current_context_id(unsigned long long* id) {
+    {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        if (!g_ctx_current || !g_ctx_id) {
+            cudaDriverEntryPointQueryResult q;
+            void* f1 = nullptr;
+            void* f2 = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault,
+                                                 &q) != cudaSuccess ||
+                q != cudaDriverEntryPointSuccess ||
+                cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault,
+                                                 &q) != cudaSuccess ||
+                q != cudaDriverEntryPointSuccess || !f1 || !f2)
+                return false;
+            g_ctx_current = reinterpret_cast<PFN_ctxGetCurrent>(f1);
+            g_ctx_id = reinterpret_cast<PFN_ctxGetId>(f2);
+        }
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return g_ctx_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device address of a __device__ variable (given by its host-side shadow) in the
+// calling thread's current context.  Cached per context ID, never per device ordinal:
+// a device reset makes a new primary context, which loads the module again and may
+// place the variable elsewhere, and a new context has a new ID.
+void* symbol_address(const void* symbol) {
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
+    if (have_id) {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        auto it = g_symbols.find({id, symbol});
+        if (it != g_symbols.end()) return it->second;
+    }
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, symbol) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (!have_id) have_id = current_context_id(&id);  // the lookup made the context current
+    if (have_id) {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        g_symbols[{id, symbol}] = p;
+    }
+    return p;
+}
+
 // Variant used before any autotuning: the fastest measured on a GB300 for the
 // configuration family (3D FP32 patch 3: z offsets in groups of three, 4 x 6 tiles,
 // faster than 4 x 8 from 64^3 to 256^3; search 11 / patch 5: groups of three, 4 x 6;
@@ -179,15 +247,7 @@ int tuned_variant(int dims, int sr, int pr, bool fp16) {
 }
 
 unsigned int* device_error_word() {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-    std::lock_guard<std::mutex> lk(g_mutex);
-    auto it = g_errword.find(dev);
-    if (it != g_errword.end()) return it->second;
-    unsigned int* p = nullptr;
-    if (cudaGetSymbolAddress((void**)&p, g_device_error_word) != cudaSuccess) return nullptr;
-    g_errword[dev] = p;
-    return p;
+    return static_cast<unsigned int*>(symbol_address(g_device_error_word));
 }
 
 cudaError_t encode_tensor_map(CUtensorMap* map, bool fp16, int rank, const uint64_t* dims,
@@ -244,6 +304,22 @@ int nlm_device_status(unsigned int* flags) {
     if (flags) *flags = v;
     if (v) return fail(NLM_ERR_DEVICE, "device error word 0x%x", v);
     return NLM_OK;
+}
+
+int nlm_test_set_fault(unsigned int bits) {
+#ifdef NLM_BOUNDS_CHECK
+    unsigned int* w = device_error_word();
+    if (!w) return fail(NLM_ERR_CUDA, "no device error word (no CUDA device?)");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
+    e = cudaMemcpy(w + 1, &bits, sizeof(bits), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "write fault-injection word");
+    return NLM_OK;
+#else
+    (void)bits;
+    return fail(NLM_ERR_UNSUPPORTED,
+                "fault injection exists only in the bounds-checked test build (libgnlm_checked.so)");
+#endif
 }
 
 int nlm_release_cached(void) {

@@ -13,10 +13,19 @@ namespace gnlm {
 // Bits of the device error word (one 32-bit word per device, see nlm_abi.cu).
 enum : unsigned int {
     DEVERR_TMA_TIMEOUT = 0x1u,     // a tile load did not complete within the wait limit
-    DEVERR_QUEUE_TIMEOUT = 0x2u,   // a persistent-kernel queue wait gave up
+    DEVERR_QUEUE_TIMEOUT = 0x2u,   // reserved: the batch work queue takes items with one
+                                   // atomicAdd and never waits, so no kernel sets this bit
     DEVERR_BAD_DESC = 0x4u,        // a work item failed its own bounds check
     DEVERR_BOUNDS = 0x8u,          // NLM_BOUNDS_CHECK build: an index range left its buffer
 };
+
+// The word after the error word is a control word that only NLM_BOUNDS_CHECK builds
+// (the test library libgnlm_checked.so) read: with FAULT_SKIP_TILE_COPY set, the CTA of
+// tile (0, 0, 0) of each 3D/2D forward or adjoint launch arms its barrier for the tile
+// copy but never issues the copy, so its bounded wait runs out exactly as it would for
+// a copy that never lands.  Nothing is in flight when that CTA gives up, and its wait
+// limit is kInjectedWaitPolls so the test does not spend the full limit.
+enum : unsigned int { FAULT_SKIP_TILE_COPY = 0x1u };
 
 // Builds compiled with -DNLM_BOUNDS_CHECK verify, once per tile or work item, that
 // the whole index range a thread is about to touch lies inside its buffer; a
@@ -47,6 +56,7 @@ __device__ __forceinline__ bool range_ok(unsigned int* errword, long long lo, lo
 // suspend the thread for a hardware-defined interval, so this bounds the wait
 // at well under a second on a healthy device.
 constexpr uint32_t kMaxWaitPolls = 1u << 22;
+constexpr uint32_t kInjectedWaitPolls = 1u << 10;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -86,9 +96,38 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Waits for phase `parity` of `bar` with an iteration limit.  Returns false if
 // the limit ran out (the caller records the error and abandons the tile).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kMaxWaitPolls; ++i)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint32_t polls = kMaxWaitPolls) {
+    for (uint32_t i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// True in the CTA that must skip its tile copy (see FAULT_SKIP_TILE_COPY); always
+// false outside NLM_BOUNDS_CHECK builds.  Uniform over the CTA.
+__device__ __forceinline__ bool inject_skip_copy(const unsigned int* errword, int bx, int by,
+                                                 int bz) {
+    if constexpr (kBoundsCheck) {
+        if (errword && (bx | by | bz) == 0)
+            return (*reinterpret_cast<const volatile unsigned int*>(errword + 1) &
+                    FAULT_SKIP_TILE_COPY) != 0;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void raise_device_error(unsigned int* word, unsigned int bits);
+
+// Waits for the tile copy of phase `parity`.  If the wait runs out, thread 0 records
+// DEVERR_TMA_TIMEOUT and waits once more for a copy that may still be landing, and the
+// caller abandons the tile (false).  `skipped`: the copy was never issued (test hook).
+__device__ __forceinline__ bool tile_copy_wait(uint64_t* bar, uint32_t parity,
+                                               unsigned int* errword, bool skipped) {
+    const uint32_t polls = skipped ? kInjectedWaitPolls : kMaxWaitPolls;
+    if (mbar_wait_bounded(bar, parity, polls)) return true;
+    if (threadIdx.x == 0) {
+        raise_device_error(errword, DEVERR_TMA_TIMEOUT);
+        mbar_wait_bounded(bar, parity, polls);
+    }
     return false;
 }
 

@@ -110,6 +110,19 @@ cudaError_t encode_tensor_map(CUtensorMap* map, bool fp16, int rank, const uint6
 // Address of the calling device's error word (see nlm_device_status).
 unsigned int* device_error_word();
 
+// Unique ID (cuCtxGetId) of the calling thread's current context; false if no
+// context is current yet or the driver entry points are unavailable.
+bool current_context_id(unsigned long long* id);
+
+// Device address of a __device__ variable, given by its host-side shadow, in the
+// calling thread's current context (cached per context ID); nullptr on failure.
+void* symbol_address(const void* symbol);
+
+// The argument checks of nlm3d_forward (pointers, dtype, radii, h, flags, extents,
+// compiled (sr, pr)); NLM_OK or the status it would return (message recorded).
+int validate_forward3d(const void* in, const void* out, int in_dtype, int X, int Y, int Z, int sr,
+                       int pr, float h, unsigned int flags);
+
 // Records `msg` as the calling thread's nlm_last_error() text; returns `code`.
 int report_error(int code, const char* msg);
 

@@ -10,20 +10,32 @@
 // must allocate that workspace.  This entry point needs neither: the staging scratch
 // lives in a fixed array compiled into this library.
 //
-// The array is kNoAllocScratchBytes (16 MiB) of device memory.  Every GPU that loads
-// the library holds it until the process exits, whether or not this entry point is
-// ever called.  A call whose staged volume needs more (padded (X+2H)(Y+2H)(Z+2H)
-// voxels, H = sr + pr, 4 bytes each in FP32; FP16 storage keeps two row-paired copies
-// of 2 bytes per voxel, so about the same; x rows rounded up to 16 bytes) is rejected
-// with NLM_ERR_WORKSPACE: for sr 3, pr 1 that is up to 152^3 (about 160^3 padded).
+// The array is kNoAllocScratchBytes (16 MiB) of device memory.  It is reserved on a
+// device when this library's module is loaded there: at context creation with eager
+// module loading, and at the latest by the first call of this entry point with CUDA's
+// default lazy loading; from then on the device holds it until the process exits.
+// A call whose staged volume needs more (padded (X+2H)(Y+2H)(Z+2H) voxels, H = sr + pr,
+// 4 bytes each in FP32; FP16 storage keeps two row-paired copies of 2 bytes per voxel,
+// so about the same; x rows rounded up to 16 bytes; the large-patch configurations add
+// two (Z, num) float pairs per voxel) is rejected with NLM_ERR_WORKSPACE: for sr 3,
+// pr 1 that is up to 152^3 (160^3 padded), FP32 or FP16 storage.
+//
+// Set-up: the first call in each context (one per device, the primary context, unless
+// the caller makes its own) looks up the array's device address with
+// cudaGetSymbolAddress while that device is current, and caches it under the
+// context's unique ID; a device reset makes a new context, which gets a new lookup
+// instead of a stale address.  That first call may also load the module, so make it
+// before any stream capture.
 //
 // Every call on a device shares the one array, so calls whose GPU work overlaps (on two
 // streams, or from two threads) race on it: serialise them, for example on one stream.
 // The array keeps whatever the last call left in it.  Nothing needs to start at zero:
-// the staging pass rewrites every byte that the NLM kernel later reads.
+// the staging pass rewrites every byte that the NLM kernels later read, and the
+// large-patch accumulators are written before they are read.
 #include <cuda_runtime.h>
 #include <stdio.h>
 
+#include <map>
 #include <mutex>
 
 #include "../../include/nlm.h"
@@ -32,7 +44,6 @@
 namespace gnlm {
 
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
-constexpr int kNoAllocMaxDevices = 64;
 
 // File-scope scratch.  In host code this name is only a host-side stand-in for the
 // symbol, not a device address: the address comes from cudaGetSymbolAddress below.
@@ -40,29 +51,35 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address of the array, per device
+std::map<unsigned long long, void*> g_noalloc_addr;  // context ID -> device address
 
-// Set-up, once per device, with that device current: look up the array's device
-// address.  Runs inside the first call on each device.
+// Device address of the array in the calling thread's current context.
 int noalloc_scratch(void** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return report_error(NLM_ERR_CUDA, "cudaGetDevice failed");
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return report_error(NLM_ERR_NO_DEVICE, "device ordinal beyond 63");
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            char msg[160];
-            snprintf(msg, sizeof(msg), "cudaGetSymbolAddress(scratch) failed: %s",
-                     cudaGetErrorString(e));
-            return report_error(NLM_ERR_CUDA, msg);
+    unsigned long long ctx = 0;
+    bool have_ctx = current_context_id(&ctx);
+    if (have_ctx) {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        auto it = g_noalloc_addr.find(ctx);
+        if (it != g_noalloc_addr.end()) {
+            *out = it->second;
+            return NLM_OK;
         }
-        g_noalloc_addr[dev] = p;
     }
-    *out = g_noalloc_addr[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        char msg[160];
+        snprintf(msg, sizeof(msg), "cudaGetSymbolAddress(scratch) failed: %s",
+                 cudaGetErrorString(e));
+        return report_error(NLM_ERR_CUDA, msg);
+    }
+    if (!have_ctx) have_ctx = current_context_id(&ctx);  // the lookup made one current
+    if (have_ctx) {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        g_noalloc_addr[ctx] = p;
+    }
+    *out = p;
     return NLM_OK;
 }
 }  // namespace
@@ -73,8 +90,11 @@ extern "C" int nlm3d_forward_noalloc(const void* d_in, int in_dtype, int X, int 
                                      int pr, float h, float* d_out, float* d_zsum,
                                      unsigned int flags, nlm_stream_t stream) {
     using namespace gnlm;
+    // The same argument checks as nlm3d_forward, before the size check, so that a bad
+    // pointer, dtype, radius, h or flag is reported as such whatever the volume's size.
+    int rc = validate_forward3d(d_in, d_out, in_dtype, X, Y, Z, sr, pr, h, flags);
+    if (rc != NLM_OK) return rc;
     const size_t need = nlm3d_workspace_bytes(X, Y, Z, sr, pr, flags);
-    if (need == 0) return report_error(NLM_ERR_INVALID_ARG, "invalid extent or radius");
     if (need > kNoAllocScratchBytes) {
         char msg[200];
         snprintf(msg, sizeof(msg),
@@ -84,8 +104,7 @@ extern "C" int nlm3d_forward_noalloc(const void* d_in, int in_dtype, int X, int 
         return report_error(NLM_ERR_WORKSPACE, msg);
     }
     void* scratch = nullptr;
-    int rc = noalloc_scratch(&scratch);
-    if (rc != NLM_OK) return rc;
+    if ((rc = noalloc_scratch(&scratch)) != NLM_OK) return rc;
     // With a caller-provided workspace nlm3d_forward neither allocates nor frees.
     return nlm3d_forward(d_in, in_dtype, X, Y, Z, sr, pr, h, d_out, d_zsum, flags, scratch,
                          kNoAllocScratchBytes, stream);

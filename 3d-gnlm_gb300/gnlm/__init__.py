@@ -70,6 +70,7 @@ def lib():
     L.nlm_last_error.restype = ctypes.c_char_p
     L.nlm_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint)]
     L.nlm_release_cached.restype = i
+    L.nlm_test_set_fault.argtypes = [u]
     L.nlm3d_workspace_bytes.argtypes = [i, i, i, i, i, u]
     L.nlm3d_workspace_bytes.restype = sz
     L.nlm3d_forward.argtypes = [vp, i, i, i, i, i, i, f, vp, vp, u, vp, sz, vp]

@@ -153,8 +153,13 @@ def fp32_peak_tflops(torch, packed=False):
     return best / 1e12
 
 
+TRAFFIC_SOURCE = ("from the committed ncu capture (profiles/traffic.txt: dram__bytes_read.sum + "
+                  "dram__bytes_write.sum of one launch of this workload), not measured in this run")
+
+
 def read_profile_traffic(kernel_key):
-    """Per-launch DRAM bytes of a kernel from profiles/traffic.txt (ncu capture)."""
+    """Per-launch DRAM bytes of a kernel from profiles/traffic.txt, an ncu capture
+    committed with the repository (a lookup, not a measurement of the current run)."""
     path = os.path.join(REPO, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
@@ -258,8 +263,18 @@ def bench_batched(torch, gnlm, reps=3):
     seq_ms = timed(sequential)
     same = max(float((a - b).abs().max()) for a, b in zip(plan.outputs, outs))
     info = plan.info()
+    # every voxel of all 64 batched outputs against the FP64 separable oracle
+    import oracle as O
+    emax, sq = 0.0, 0.0
+    for (t, sr, pr, h), o in zip(vols, plan.outputs):
+        ref = O.nlm3d(t.cpu().numpy(), sr, pr, h, dtype=np.float64)
+        d = o.cpu().numpy().astype(np.float64) - ref
+        emax = max(emax, float(np.abs(d).max()))
+        sq += float((d * d).sum())
     plan.close()
     return {"volumes": len(vols), "voxels": nvox, "work_items": info["items"],
+            "max_abs_err_vs_fp64": emax, "rms_err_vs_fp64": (sq / nvox) ** 0.5,
+            "error_sample": "every voxel of the 64 volumes vs the FP64 separable oracle",
             "value": round(nvox / (batch_ms * 1e-3) / 1e6, 2), "ms": round(batch_ms, 3),
             "sequential_value": round(nvox / (seq_ms * 1e-3) / 1e6, 2),
             "sequential_ms": round(seq_ms, 3), "speedup_vs_sequential": round(seq_ms / batch_ms, 3),
@@ -285,7 +300,12 @@ def bench_2d(torch, gnlm, reps=5):
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
     t = min(ms)
+    import oracle as O
+    d = out.cpu().numpy().astype(np.float64) - O.nlm2d(im, 5, 2, 0.08, dtype=np.float64)
     return {"shape": [2048, 2048], "search_radius": 5, "patch_radius": 2, "ms": round(t, 4),
+            "max_abs_err_vs_fp64": float(np.abs(d).max()),
+            "rms_err_vs_fp64": float(np.sqrt(np.mean(d * d))),
+            "error_sample": "every pixel vs the FP64 separable oracle",
             "value": round(2048 * 2048 / (t * 1e-3) / 1e6, 1), "unit": "Mpixel/s",
             "tflops": round(10 * 121 * 2048 * 2048 / (t * 1e-3) / 1e12, 2), "variant": best,
             "autotune_ms": [round(v, 4) for v in tune]}
@@ -315,7 +335,18 @@ def bench_large_patch(torch, gnlm, reps=3):
     nvox = shape[0] * shape[1] * shape[2]
     pairs = nvox * (2 * sr + 1) ** 3
     gnlm.set_variant(3, sr, pr, -1)
+    # FP64 oracle on 16^3 boxes at the 8 corners, the 6 face centres and the centre
+    import oracle as O
+    blk = (16, 16, 16)
+    origins = O.border_blocks(shape, blk)
+    ref = O.nlm3d_blocks(v, sr, pr, 0.05, origins, blk)
+    g = out.cpu().numpy()
+    d = np.stack([g[z:z + 16, y:y + 16, x:x + 16] for (z, y, x) in origins]).astype(np.float64) - ref
     return {"shape": list(shape), "search_radius": sr, "patch_radius": pr, "ms": round(t, 3),
+            "max_abs_err_vs_fp64": float(np.abs(d).max()),
+            "rms_err_vs_fp64": float(np.sqrt(np.mean(d * d))),
+            "error_sample": f"{len(origins)} boxes of 16^3 (8 corners, 6 face centres, centre; "
+                            f"{d.size} voxels) vs the FP64 separable oracle",
             "value": round(nvox / (t * 1e-3) / 1e6, 2), "unit": "Mvoxel/s",
             "gpairs_per_s": round(pairs / (t * 1e-3) / 1e9, 1),
             "tflops": round(FLOPS_PER_PAIR * pairs / (t * 1e-3) / 1e12, 2),
@@ -355,6 +386,17 @@ def bench_adjoint(torch, gnlm, peak_tflops, steps=50, reps=20):
         fwd_t.append(ev[0].elapsed_time(ev[1]))
         adj_t.append(ev[1].elapsed_time(ev[2]))
     fwd_ms, adj_ms = statistics.median(fwd_t), statistics.median(adj_t)
+    # the kernels' gradients against FP64 central differences: dL/dv on 256 voxels
+    # (corners, faces, random), dL/dh from two full FP64 forwards
+    import oracle as O
+    g64 = g.cpu().numpy().astype(np.float64)
+    vox = O.fd_sample_voxels((128, 128, 128), 256, seed=6)
+    fd = O.fd_voxel_grad(noisy, SR, PR, 0.05, g64, vox, eps=1e-5)
+    gin_h = gin.cpu().numpy()
+    fd_rel_v = float(np.abs(np.array([gin_h[i] for i in vox], np.float64) - fd).max()
+                     / np.abs(fd).max())
+    fdh = O.fd_h_grad(noisy, SR, PR, 0.05, g64, eps=1e-6)
+    fd_rel_h = abs(float(hg.item()) - fdh) / abs(fdh)
     padded = (128 + 2 * (SR + PR)) ** 3
     adj_tflops = ADJ_FLOPS_PER_PAIR * OFFSETS * padded / (adj_ms * 1e-3) / 1e12
     # h fit: 50 steps of normalised gradient descent on MSE(out(h), clean)
@@ -382,6 +424,9 @@ def bench_adjoint(torch, gnlm, peak_tflops, steps=50, reps=20):
             "fwd_ms": round(fwd_ms, 3), "adjoint_ms": round(adj_ms, 3),
             "fwd_adjoint_ms_per_step": round(fwd_ms + adj_ms, 3), "timing": f"median of {reps}",
             "fwd_variant": fwd_variant,
+            "grad_rel_err_vs_fp64_fd": {"dL_dv": fd_rel_v, "dL_dh": fd_rel_h,
+                                        "sample": "256 voxels (8 corners, 6 faces, 242 random), "
+                                                  "max |adjoint - FD| / max |FD|; h: relative"},
             "adjoint_tflops": round(adj_tflops, 3),
             "adjoint_frac_fp32_peak": round(adj_tflops / peak_tflops, 4) if peak_tflops else None,
             "adjoint_algorithmic": f"{ADJ_FLOPS_PER_PAIR} flops x {OFFSETS} offsets x {padded} "
@@ -509,23 +554,36 @@ def run_gnlm(args):
     e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.steps, "cuda")
     e2e_value = replica_throughput(nvox, world, e2e_s) / 1e6
     assert np.array_equal(a_out, out32.cpu().numpy()), "host path disagrees with device path"
+    # the FP16-storage form end to end from an FP16 host volume: half the host->device bytes
+    h_in16 = torch.from_numpy(vol.astype(np.float16)).pin_memory()
+    a_in16 = h_in16.numpy()
+    h_out16 = torch.empty(SHAPE, dtype=torch.float32).pin_memory()
+    a_out16 = h_out16.numpy()
+    for _ in range(max(1, args.warmup)):
+        gnlm.nlm3d_forward_host(a_in16, SR, PR, H, fp16_storage=True, out=a_out16)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gnlm.nlm3d_forward_host(a_in16, SR, PR, H, fp16_storage=True, out=a_out16)
+    e2e16_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.steps, "cuda")
+    e2e16_value = replica_throughput(nvox, world, e2e16_s) / 1e6
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return 0
 
-    # accuracy against the FP64 oracle on spot blocks (corners + interior)
+    # accuracy of every voxel against the FP64 separable oracle
     import oracle as O
-    o32, o16 = out32.cpu().numpy(), out16.cpu().numpy()
-    d32, d16 = [], []
-    for (z0, y0, x0) in [(0, 0, 0), (248, 248, 248), (124, 60, 200), (40, 180, 8)]:
-        ref = O.nlm3d_region(vol, SR, PR, H, (z0, y0, x0), (8, 8, 8))
-        d32.append((o32[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8] - ref).ravel())
-        d16.append((o16[z0:z0 + 8, y0:y0 + 8, x0:x0 + 8] - ref).ravel())
-    d32, d16 = np.concatenate(d32).astype(np.float64), np.concatenate(d16).astype(np.float64)
-    err32, err16 = float(np.abs(d32).max()), float(np.abs(d16).max())
-    rms32, rms16 = float(np.sqrt(np.mean(d32 ** 2))), float(np.sqrt(np.mean(d16 ** 2)))
+    ref64 = O.nlm3d(vol, SR, PR, H, dtype=np.float64)
+    d32 = out32.cpu().numpy().astype(np.float64) - ref64
+    err32, rms32 = float(np.abs(d32).max()), float(np.sqrt(np.mean(d32 * d32)))
+    del d32
+    d16 = out16.cpu().numpy().astype(np.float64) - ref64
+    err16, rms16 = float(np.abs(d16).max()), float(np.sqrt(np.mean(d16 * d16)))
+    # FP16 host input: the volume itself rounded to FP16 before the call
+    d16h = a_out16.astype(np.float64) - ref64
+    err16h, rms16h = float(np.abs(d16h).max()), float(np.sqrt(np.mean(d16h * d16h)))
+    del d16, d16h, ref64
 
     peak = fp32_peak_tflops(torch)
     peak_x2 = fp32_peak_tflops(torch, packed=True)
@@ -556,6 +614,7 @@ def run_gnlm(args):
                      "peak": round(peak, 3), "unit": "TFLOP/s",
                      "frac": round(achieved / peak, 4) if peak else None,
                      "traffic": traffic,
+                     "traffic_source": TRAFFIC_SOURCE,
                      "kernel": f"{kname}<3,1> (FP32 variant {tuned32[0]})",
                      "peak_source": "FFMA probe kernel measured in this run (FP32 pipe; "
                                     "MEASURED_PEAKS.json has HBM and bf16 only)",
@@ -565,6 +624,7 @@ def run_gnlm(args):
                              "peak": round(hbm_peak, 1), "unit": "GB/s",
                              "frac": round(stage_gbs / hbm_peak, 4), "peak_source": hbm_src,
                              "traffic": read_profile_traffic("stage_kernel"),
+                             "traffic_source": TRAFFIC_SOURCE,
                              "algorithmic": "input read once + padded volume written once "
                                             f"({staging_bytes(SHAPE, SR, PR)} bytes)"},
         "autotune": {"fp32": {"chosen": tuned32[0], "ms": [round(t, 4) for t in tuned32[1]]},
@@ -576,8 +636,17 @@ def run_gnlm(args):
         "forms": {"fp32": {"value": round(value, 2), "max_abs_err_vs_fp64": err32,
                            "rms_err_vs_fp64": rms32},
                   "fp16_storage": {"value": round(fp16_value, 2), "max_abs_err_vs_fp64": err16,
-                                   "rms_err_vs_fp64": rms16},
-                  "error_sample": "4 blocks of 8^3 (two corners, two interior) vs the FP64 direct form",
+                                   "rms_err_vs_fp64": rms16,
+                                   "e2e": {"value": round(e2e16_value, 2), "unit": UNIT,
+                                           "h2d_bytes_per_step": int(a_in16.nbytes),
+                                           "d2h_bytes_per_step": int(a_out16.nbytes),
+                                           "input": "FP16 host volume (the FP32 phantom rounded)",
+                                           "max_abs_err_vs_fp64": err16h,
+                                           "rms_err_vs_fp64": rms16h},
+                                   "faster_than_fp32": {
+                                       "device_resident": fp16_value > value,
+                                       "e2e": e2e16_value > e2e_value}},
+                  "error_sample": "every voxel of the 256^3 output vs the FP64 separable oracle",
                   "batched": batched},
         "adjoint": adjoint,
         "nlm2d": image2d,

@@ -74,11 +74,20 @@ const char* nlm_last_error(void);
 
 /* Synchronises the current device, then reads and clears the device-side error
  * word that kernels set when a bounded wait gives up.  *flags receives the word
- * (0 = no error; 0x1 a tile copy timed out, 0x2 a persistent-kernel queue wait gave
- * up, 0x4 a batch work item failed its own check, 0x8 an index range left its
- * buffer — reported only by the NLM_BOUNDS_CHECK build, libgnlm_checked.so).
+ * (0 = no error; 0x1 a tile copy timed out, 0x2 reserved (the batch work queue
+ * never waits, so no kernel sets it), 0x4 a batch work item failed its own check,
+ * 0x8 an index range left its buffer — reported only by the NLM_BOUNDS_CHECK build,
+ * libgnlm_checked.so).
  * Returns NLM_OK, or NLM_ERR_DEVICE when the word was set. */
 int nlm_device_status(unsigned int* flags);
+
+/* Test hook (no counterpart in the reference): in the bounds-checked test build,
+ * libgnlm_checked.so, bits = 0x1 makes the first tile (0, 0, 0) of every later 3D/2D
+ * forward and adjoint launch on the current device skip its tile copy, so its bounded
+ * wait runs out and the kernel reports 0x1 in the device error word instead of
+ * hanging; that tile's outputs are left unwritten.  bits = 0 turns it off.  The
+ * production library (libgnlm.so) returns NLM_ERR_UNSUPPORTED and changes nothing. */
+int nlm_test_set_fault(unsigned int bits);
 
 /* Frees the library-cached workspaces and host-path buffers of every device (the
  * reference allocates and frees its buffers inside every NL_Means call,

@@ -192,6 +192,45 @@ DEFINE_REGION(float, f32, expf)
 DEFINE_REGION(double, f64, exp)
 
 /*
+ * Separable form on many boxes of one full volume, each nx x ny x nz with its origin
+ * (x, y, z) at origins[3 b .. 3 b + 2]; out holds the boxes one after another.  Each
+ * box plus its halo H = sr + pr is gathered from the volume through the REFLECT_101
+ * map and the separable core runs on that padded block: an output depends only on
+ * inputs within H of it, so the box equals the full-volume separable result.  The
+ * per-(voxel, offset) cost is O(patch width) instead of the direct form's O(patch
+ * volume), which makes FP64 checks of patch-17^3 outputs affordable.  OpenMP over
+ * boxes (the core runs single-threaded inside).
+ */
+#define DEFINE_BLOCKS_SEP(T, SUF)                                                              \
+    void oracle_nlm3d_blocks_sep_##SUF(const T* v, int X, int Y, int Z, int sr, int pr, T h,  \
+                                       int nblk, const int* origins, int nx, int ny, int nz,  \
+                                       T* out)                                                \
+    {                                                                                          \
+        const long H = sr + pr;                                                                \
+        const long xp = nx + 2 * H, yp = ny + 2 * H, zp = nz + 2 * H;                          \
+        _Pragma("omp parallel for schedule(dynamic, 1)")                                       \
+        for (int b = 0; b < nblk; ++b) {                                                       \
+            const long x0 = origins[3 * b], y0 = origins[3 * b + 1], z0 = origins[3 * b + 2];  \
+            T* blk = (T*)malloc(sizeof(T) * xp * yp * zp);                                     \
+            for (long zz = 0; zz < zp; ++zz) {                                                 \
+                const long sz = oracle_reflect101(z0 + zz - H, Z);                             \
+                for (long yy = 0; yy < yp; ++yy) {                                             \
+                    const long sy = oracle_reflect101(y0 + yy - H, Y);                         \
+                    const T* row = v + (sz * Y + sy) * (long)X;                                \
+                    T* dst = blk + (zz * yp + yy) * xp;                                        \
+                    for (long xx = 0; xx < xp; ++xx)                                           \
+                        dst[xx] = row[oracle_reflect101(x0 + xx - H, X)];                      \
+                }                                                                              \
+            }                                                                                  \
+            core3d_sep##SUF(blk, xp, yp, nx, ny, nz, sr, pr, h,                                \
+                            out + (long)b * nx * ny * nz, NULL, nz);                           \
+            free(blk);                                                                         \
+        }                                                                                      \
+    }
+DEFINE_BLOCKS_SEP(float, f32)
+DEFINE_BLOCKS_SEP(double, f64)
+
+/*
  * Legacy layout (3DNLM/main.h:6, 3DNLM/main.cu:7607-7680): the input is already
  * padded by the caller, unsigned char [Z+SS+NS-2][Y+SS+NS-2][X+SS+NS-2];
  * output float [Z][Y][X]; h on the 0..255 scale (PARAMETER).
@@ -336,4 +375,79 @@ void oracle_nlm3d_adjoint_f64(const double* v, int X, int Y, int Z, int sr, int 
     free(gpad_all);
     free(gh_t);
     free(vp);
+}
+
+/*
+ * FP64 central finite differences of L(v) = sum_p g_p out_p(v) with respect to n
+ * chosen voxels (test infrastructure for the adjoint; no counterpart in the
+ * reference).  For voxel i at idx[3 i .. 3 i + 2] = (x, y, z):
+ *   fd[i] = (L(v + eps e_i) - L(v - eps e_i)) / (2 eps),
+ * where only the outputs within H = sr + pr of the voxel on every axis change (the
+ * REFLECT_101 images of a voxel within H of a face fall inside that box), so L is
+ * summed over that box with the direct form.  OpenMP over voxels; each thread
+ * perturbs a private copy of the volume.
+ */
+static double fd_box_loss(const double* v, int X, int Y, int Z, int m, int n, double h,
+                          const double* g, int bx0, int by0, int bz0, int bx1, int by1, int bz1)
+{
+    const double P = (double)(2 * n + 1) * (2 * n + 1) * (2 * n + 1);
+    double L = 0;
+    for (int z = bz0; z <= bz1; ++z)
+        for (int y = by0; y <= by1; ++y)
+            for (int x = bx0; x <= bx1; ++x) {
+                double num = 0, zs = 0;
+                for (int oz = -m; oz <= m; ++oz)
+                    for (int oy = -m; oy <= m; ++oy)
+                        for (int ox = -m; ox <= m; ++ox) {
+                            double D = 0;
+                            for (int tz = -n; tz <= n; ++tz)
+                                for (int ty = -n; ty <= n; ++ty)
+                                    for (int tx = -n; tx <= n; ++tx) {
+                                        const double a =
+                                            v[(oracle_reflect101(z + tz, Z) * Y +
+                                               oracle_reflect101(y + ty, Y)) * (long)X +
+                                              oracle_reflect101(x + tx, X)];
+                                        const double b =
+                                            v[(oracle_reflect101(z + oz + tz, Z) * Y +
+                                               oracle_reflect101(y + oy + ty, Y)) * (long)X +
+                                              oracle_reflect101(x + ox + tx, X)];
+                                        D += (a - b) * (a - b);
+                                    }
+                            const double w = exp(-(D / P) / (h * h));
+                            zs += w;
+                            num += w * v[(oracle_reflect101(z + oz, Z) * Y +
+                                          oracle_reflect101(y + oy, Y)) * (long)X +
+                                         oracle_reflect101(x + ox, X)];
+                        }
+                L += g[((long)z * Y + y) * X + x] * (num / zs);
+            }
+    return L;
+}
+
+void oracle_nlm3d_fd_grad_f64(const double* v, int X, int Y, int Z, int sr, int pr, double h,
+                              const double* g, int nvox, const int* idx, double eps,
+                              double* fd)
+{
+    const int H = sr + pr;
+    const size_t N = (size_t)X * Y * Z;
+#pragma omp parallel
+    {
+        double* w = (double*)malloc(sizeof(double) * N);
+        memcpy(w, v, sizeof(double) * N);
+#pragma omp for schedule(dynamic, 1)
+        for (int i = 0; i < nvox; ++i) {
+            const int x = idx[3 * i], y = idx[3 * i + 1], z = idx[3 * i + 2];
+            const int bx0 = x - H > 0 ? x - H : 0, bx1 = x + H < X - 1 ? x + H : X - 1;
+            const int by0 = y - H > 0 ? y - H : 0, by1 = y + H < Y - 1 ? y + H : Y - 1;
+            const int bz0 = z - H > 0 ? z - H : 0, bz1 = z + H < Z - 1 ? z + H : Z - 1;
+            const long k = ((long)z * Y + y) * X + x;
+            w[k] = v[k] + eps;
+            const double Lp = fd_box_loss(w, X, Y, Z, sr, pr, h, g, bx0, by0, bz0, bx1, by1, bz1);
+            w[k] = v[k] - eps;
+            const double Lm = fd_box_loss(w, X, Y, Z, sr, pr, h, g, bx0, by0, bz0, bx1, by1, bz1);
+            w[k] = v[k];
+            fd[i] = (Lp - Lm) / (2 * eps);
+        }
+        free(w);
+    }
 }

@@ -12,7 +12,8 @@
 # With --if-present the script exits quietly when the sources are not there (the
 # cubins then come from an earlier build, or the tests that need them skip).
 set -euo pipefail
-REF=${REF:-/root/reference}
+# The reference checkout: $REF, else a directory named "reference" beside the repository.
+REF=${REF:-$(cd "$(dirname "$0")/../.." && pwd)/reference}
 if [ "${1:-}" = "--if-present" ] && [ ! -d "$REF/3DNLM" ]; then exit 0; fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"

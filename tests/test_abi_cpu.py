@@ -44,6 +44,30 @@ def test_legacy_shim_exports_reference_signatures(gnlm_lib):
     assert hasattr(legacy, "_ZN16NLMeansProcessor8NL_MeansEPhPfiiiiii")
 
 
+def test_noalloc_checks_arguments_before_its_size_limit(L):
+    """A bad pointer, dtype, h or flag on a volume too large for the allocation-free
+    entry point's array is reported as the bad argument, not as a size problem (the
+    checks run on the host; no device work is issued)."""
+    P = ctypes.c_void_p
+    big = (400, 400, 400)
+    assert L.nlm3d_workspace_bytes(*big, 3, 1, 0) > 16 << 20
+    one = P(256)  # never dereferenced: every call below fails its host checks first
+    calls = [(None, gnlm.NLM_F32, 0.05, 0), (one, 7, 0.05, 0), (one, gnlm.NLM_F32, -1.0, 0),
+             (one, gnlm.NLM_F32, 0.05, 0x80)]
+    for d_in, dt, h, flags in calls:
+        rc = L.nlm3d_forward_noalloc(d_in, dt, *big, 3, 1, h, one, None, flags, None)
+        assert rc == gnlm.NLM_ERR_INVALID_ARG, (d_in, dt, h, flags, gnlm.last_error())
+    rc = L.nlm3d_forward_noalloc(one, gnlm.NLM_F32, *big, 9, 1, 0.05, one, None, 0, None)
+    assert rc == gnlm.NLM_ERR_UNSUPPORTED
+
+
+def test_fault_hook_is_inert_in_the_production_build(L):
+    """nlm_test_set_fault exists only to drive the bounded waits of the checked test
+    build; the production library refuses it before touching any device."""
+    assert L.nlm_test_set_fault(1) == gnlm.NLM_ERR_UNSUPPORTED
+    assert "test build" in gnlm.last_error()
+
+
 def test_version(L):
     assert b"sm_103a" in L.nlm_version()
 

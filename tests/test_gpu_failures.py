@@ -62,3 +62,32 @@ def test_bounds_checked_build_is_clean_and_identical(torch_cuda, gnlm_lib, tmp_p
     assert sorted(got.files) == sorted(ref)
     for k, v in ref.items():
         assert np.array_equal(got[k], v), k
+
+
+def test_bounded_tile_copy_waits_run_out_and_report(torch_cuda, gnlm_lib):
+    """Every kernel family's bounded tile-copy wait is driven to its limit in the
+    checked test build (tests/fault_cases.py, a child process): the call returns, the
+    device error word reports 0x1 (tile copy timed out), and once injection is off the
+    next call is clean and matches the FP64 oracle.  No GPU fault is involved: the
+    injected CTA never issues its copy, so nothing is in flight when it gives up."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    if not os.path.exists(gnlm_lib.CHECKED_LIB_PATH):
+        pytest.skip("checked build not present")
+    env = dict(os.environ, GNLM_LIB=gnlm_lib.CHECKED_LIB_PATH)
+    here = os.path.dirname(os.path.abspath(__file__))
+    proc = subprocess.run([sys.executable, os.path.join(here, "fault_cases.py")], env=env,
+                          capture_output=True, text=True, timeout=600)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    res = json.loads(proc.stdout.strip().splitlines()[-1])
+    assert res["lib"].endswith("libgnlm_checked.so")
+    assert set(res["cases"]) == {"3d_fp32", "3d_fp16_storage", "2d", "batched", "adjoint"}
+    for name, r in res["cases"].items():
+        assert r["set"] == 0 and r["unset"] == 0, (name, r)
+        assert r["status"] == gnlm_lib.NLM_ERR_DEVICE and r["flags"] == 0x1, (name, r)
+        assert r["after_status"] == 0 and r["after_flags"] == 0, (name, r)
+    assert res["after_err_vs_fp64"] <= 1e-5
+    assert res["final_status"] == [0, 0]

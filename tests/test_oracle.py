@@ -32,6 +32,25 @@ def test_direct_vs_separable_3d(sr, pr):
     assert np.abs(c - d).max() < 1e-12
 
 
+@pytest.mark.parametrize("sr,pr,shape,size", [(2, 2, (24, 30, 36), (6, 7, 8)),
+                                               (1, 3, (12, 14, 10), (5, 4, 3))])
+def test_block_separable_form_matches_full_volume(sr, pr, shape, size):
+    """Boxes at every corner, face centre and the centre, each with its halo gathered
+    through REFLECT_101, against the full-volume separable and direct forms."""
+    v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=6, sigma=0.05, seed=3, radii=(2, 8))
+    full = O.nlm3d(v, sr, pr, 0.05, dtype=np.float64)
+    origins = O.border_blocks(shape, size)
+    assert len(set(origins)) == 15
+    blocks = O.nlm3d_blocks(v, sr, pr, 0.05, origins, size)
+    nz, ny, nx = size
+    for b, (z, y, x) in zip(blocks, origins):
+        assert np.abs(b - full[z:z + nz, y:y + ny, x:x + nx]).max() < 1e-14
+    d = O.nlm3d_region(v, sr, pr, 0.05, origins[7], size)
+    assert np.abs(d - blocks[7]).max() < 1e-14
+    b32 = O.nlm3d_blocks(v, sr, pr, 0.05, origins[:2], size, dtype=np.float32)
+    assert np.abs(b32 - blocks[:2]).max() < 1e-6
+
+
 def test_constant_volume_is_fixed_point():
     k = np.full((7, 8, 9), 0.37, np.float32)
     assert np.abs(O.nlm3d(k, 3, 1, 0.05) - 0.37).max() < 2e-6
