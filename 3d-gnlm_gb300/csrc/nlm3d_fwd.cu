@@ -183,17 +183,26 @@ static bool small_case(int sr, int pr) {
     return false;
 }
 
-// Pairs without a register-brick instance run on the large-patch kernel (FP32
-// staging only).
+// Pairs without a register-brick instance run on the large-patch kernel (FP32 or
+// plain FP16 staging).
 bool nlm3d_fwd_large_patch(int sr, int pr, bool fp16) {
-    return !fp16 && !small_case(sr, pr) && nlm3d_lp_supported(sr, pr);
+    (void)fp16;
+    return !small_case(sr, pr) && nlm3d_lp_supported(sr, pr);
 }
 
-// Two (Z, num) accumulator buffers: the large-patch launcher may split each tile's
-// passes into two halves (nlm3d_lp_split).
+// Two accumulator buffers: the large-patch launcher may split each tile's passes into
+// two halves (nlm3d_lp_split).  (Z, num) float2 per voxel, or with FP16 storage the
+// Kahan pairs (Z, num, cZ, cnum) float4.
 size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16) {
     if (!nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
-    return align_up(2 * (size_t)X * Y * Z * sizeof(float2), kAlign);
+    return align_up(2 * (size_t)X * Y * Z * (fp16 ? sizeof(float4) : sizeof(float2)), kAlign);
+}
+
+Staging staging3d(int X, int Y, int Z, int sr, int pr, bool fp16) {
+    const int H = sr + pr;
+    if (!fp16) return make_staging(X, Y, Z, H, H, false);
+    return nlm3d_fwd_large_patch(sr, pr, true) ? make_staging(X, Y, Z, H, H, true)
+                                               : make_staging_pairs(X, Y, Z, H);
 }
 
 int nlm3d_fwd_tile_z(int sr, int pr, bool fp16, int v) {
@@ -218,10 +227,9 @@ cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int 
     GNLM_FWD3D_CASES(X_)
 #undef X_
     if (nlm3d_fwd_large_patch(sr, pr, fp16)) {
-        float2* acc = reinterpret_cast<float2*>(static_cast<char*>(const_cast<void*>(staged)) +
-                                                st.bytes());
-        return launch_nlm3d_lp(st, staged, sr, pr, variant, inv_scale, out, zsum, acc, errword,
-                               stream, zt0, zt1);
+        void* acc = static_cast<char*>(const_cast<void*>(staged)) + st.bytes();
+        return launch_nlm3d_lp(st, staged, sr, pr, fp16, variant, inv_scale, out, zsum, acc,
+                               errword, stream, zt0, zt1);
     }
     return cudaErrorNotSupported;
 }

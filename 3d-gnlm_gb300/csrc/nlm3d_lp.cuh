@@ -29,38 +29,56 @@
 // idle; the launcher may then split each tile's passes into two halves run by
 // two CTAs with separate accumulator buffers, and a combine kernel adds the two
 // halves (always in the same order) and writes num / Z.
+//
+// Storage type T: float, or __half for the FP16-storage form (the staged volume and
+// the TMA plane boxes hold FP16, halving their bytes; every difference, square and
+// sum is FP32, and the per-pass weight sums are added across passes with Kahan
+// compensation, the (Z, num) accumulator then holding (Z, num, cZ, cnum)).  TMA needs
+// 16-byte aligned box starts and widths, so for FP16 the boxes start 8 elements
+// before the tile (candidate box) or on the 8-element boundary below the first
+// halo group (reference box) and the in-box column offsets CB and RO absorb that.
 #pragma once
+
+#include <algorithm>
 
 #include "nlm3d_tile.cuh"
 #include "nlm_device.cuh"
+#include "nlm_internal.h"
 
 namespace gnlm {
 
-template <int M, int N>
+template <int M, int N, typename T>
 struct Lp3d {
+    static constexpr int ES = (int)sizeof(T);  // bytes per staged element
+    static constexpr int EA = 16 / ES;         // elements per 16 bytes (TMA alignment)
+    static constexpr bool KAHAN = ES == 2;     // FP16-storage form: compensated pass sums
     static constexpr int K = 2 * M + 1;        // x offsets per pass
     static constexpr int CX = 32;              // output columns per CTA
     static constexpr int CY = 16;              // output rows per CTA
     static constexpr int H = M + N;
     static constexpr int HX = CX + 2 * N;      // halo columns
     static constexpr int HY = CY + 2 * N;      // halo rows
-    // Boxes start at padded column X0 - 4 (16-byte aligned); box column i is
-    // padded column X0 - 4 + i, halo column xh is i = 4 + M + xh.
-    static constexpr int R = (M + 3) / 4;      // candidate float4s either side of a group
+    // Column i of the 4-column group layout is padded column X0 - 4 + i (halo column
+    // xh is i = 4 + M + xh).  The candidate box starts at padded column X0 - 4 - CB and
+    // the reference box at X0 - 4 + 4*G0 - RO (16-byte aligned starts), so layout
+    // column i sits at candidate-box column i + CB.
+    static constexpr int R = (M + 3) / 4;      // candidate 4-column groups either side
     static constexpr int G0 = 1 + M / 4;       // first 4-column group holding a halo column
     static constexpr int G1 = (4 + M + HX + 3) / 4;
     static constexpr int NG = G1 - G0;         // groups per halo row
     static constexpr int MA = M % 4;           // halo column 0 in an Sz row
-    static constexpr int BWR = 4 * NG;         // reference box width (columns 4*G0 ..)
-    static constexpr int BWC = 4 * (G1 + R);   // candidate box width (columns 0 ..)
-    static constexpr int PSZ = (BWR % 8 == 4) ? BWR : BWR + 4;  // Sz row pitch, PSZ/4 odd
+    static constexpr int CB = EA - 4;          // 0 (FP32) or 4 (FP16)
+    static constexpr int RO = (4 * G0 - 4) % EA;
+    static constexpr int BWR = cround(4 * NG + RO, EA);     // reference box width (elements)
+    static constexpr int BWC = cround(4 * (G1 + R) + CB, EA);  // candidate box width
+    static constexpr int PSZ = ((4 * NG) % 8 == 4) ? 4 * NG : 4 * NG + 4;  // Sz pitch, PSZ/4 odd
     static constexpr int PSX = 36;             // Sx row pitch (32 used), PSX/4 odd
     static constexpr int THREADS = 512;
     static constexpr int NA = 16 * HY;         // stage A threads (16 per halo row, NG used)
     static constexpr int NB = K * HY;          // stage B items (k, halo row)
     static constexpr int NC = K * CX;          // stage C items (k, column)
-    static constexpr int REF_TX = BWR * HY * 4;    // bytes of a reference plane box
-    static constexpr int CAND_TX = BWC * HY * 4;   // bytes of a candidate plane box
+    static constexpr int REF_TX = BWR * HY * ES;   // bytes of a reference plane box
+    static constexpr int CAND_TX = BWC * HY * ES;  // bytes of a candidate plane box
     static constexpr int REF_SLOT = cround(REF_TX, 128);
     static constexpr int CAND_SLOT = cround(CAND_TX, 128);
     static constexpr int ABUF = 2 * REF_SLOT + 2 * CAND_SLOT;  // entering/leaving ref + cand
@@ -76,9 +94,10 @@ struct Lp3d {
     static_assert(CX == 32 && CY == 16, "stage B/C split outputs into two runs");
     static_assert(CX * CY == THREADS, "one stage-D voxel per thread");
     static_assert(4 * R >= M, "candidate window covers the x offsets");
-    static_assert(BWR >= MA + HX, "Sz row covers the halo");
+    static_assert(4 * NG >= MA + HX, "Sz row covers the halo");
     static_assert(BWC <= 256 && BWR <= 256 && HY <= 256, "TMA box dimension > 256");
-    static_assert(4 + N + 31 + 2 * M < BWC, "stage D candidates inside the box");
+    static_assert(CB + 4 + N + 31 + 2 * M < BWC, "stage D candidates inside the box");
+    static_assert((BWR * ES) % 16 == 0 && (BWC * ES) % 16 == 0, "TMA box rows of 16-byte units");
     static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 };
 
@@ -91,17 +110,34 @@ struct LpArgs {
     int nsplit;       // 1: a CTA makes every pass; 2: each half of the passes
     size_t part_stride;  // float2 pairs per accumulator buffer (X * Y * Z)
     float inv_scale;
-    float2* acc;      // (Z, num) pairs, [nsplit][Z][Y][X]
+    void* acc;        // [nsplit][Z][Y][X] of (Z, num) float2, or (Z, num, cZ, cnum) float4
+                      // for the FP16-storage form
     float* out;
     float* zsum;
     unsigned int* errword;
 };
 
-template <int M, int N>
+// Four consecutive staged elements (8 bytes of FP16 or 16 of FP32) as FP32.
+__device__ __forceinline__ float4 load4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 load4(const __half* p) {
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    const float2 lo = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 hi = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+// Adds a pass's (Z, num) increment to a Kahan pair (sum, compensation) per component.
+__device__ __forceinline__ float4 kahan_step(float4 acc, float dz, float dn) {
+    const float yz = dz - acc.z, yn = dn - acc.w;
+    const float tz = acc.x + yz, tn = acc.y + yn;
+    return make_float4(tz, tn, (tz - acc.x) - yz, (tn - acc.y) - yn);
+}
+
+template <int M, int N, typename Elem>
 __global__ void __launch_bounds__(512, 1)
     nlm3d_lp_kernel(const __grid_constant__ CUtensorMap mapR,
                     const __grid_constant__ CUtensorMap mapC, const LpArgs a) {
-    using C = Lp3d<M, N>;
+    using C = Lp3d<M, N, Elem>;
     extern __shared__ __align__(128) unsigned char smem[];
     float* Szb = reinterpret_cast<float*>(smem + C::SZ_OFF);
     float* Sxb = reinterpret_cast<float*>(smem + C::SX_OFF);
@@ -118,7 +154,8 @@ __global__ void __launch_bounds__(512, 1)
     // This CTA's passes [pb, pb + P) of the (2sr+1)^2, and its accumulator buffer.
     const int pb = part * (C::K * C::K) / a.nsplit;
     const int P = (part + 1) * (C::K * C::K) / a.nsplit - pb;
-    float2* const acc = a.acc + part * a.part_stride;
+    float2* const acc = static_cast<float2*>(a.acc) + part * a.part_stride;
+    float4* const acck = static_cast<float4*>(a.acc) + part * a.part_stride;
     // A pass is N warm-up steps, each adding two planes of the first window
     // (padded planes Z0+M .. Z0+M+2N-1), then TZc output steps: output plane
     // Z0+q adds padded plane Z0+M+2N+q and, for q >= 1, drops Z0+M+q-1.
@@ -147,12 +184,12 @@ __global__ void __launch_bounds__(512, 1)
         const int xr = X0 - 4 + 4 * C::G0, yr = Y0 + M;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&barA[b], (p1 >= 0 ? 2u : 1u) * (C::REF_TX + C::CAND_TX));
-        tma_load_3d(base, &mapR, xr, yr, p0, &barA[b]);
-        tma_load_3d(base + 2 * C::REF_SLOT, &mapC, X0 - 4, yr + oy, p0 + oz, &barA[b]);
+        tma_load_3d(base, &mapR, xr - C::RO, yr, p0, &barA[b]);
+        tma_load_3d(base + 2 * C::REF_SLOT, &mapC, X0 - 4 - C::CB, yr + oy, p0 + oz, &barA[b]);
         if (p1 >= 0) {
-            tma_load_3d(base + C::REF_SLOT, &mapR, xr, yr, p1, &barA[b]);
-            tma_load_3d(base + 2 * C::REF_SLOT + C::CAND_SLOT, &mapC, X0 - 4, yr + oy, p1 + oz,
-                        &barA[b]);
+            tma_load_3d(base + C::REF_SLOT, &mapR, xr - C::RO, yr, p1, &barA[b]);
+            tma_load_3d(base + 2 * C::REF_SLOT + C::CAND_SLOT, &mapC, X0 - 4 - C::CB, yr + oy,
+                        p1 + oz, &barA[b]);
         }
     };
     // Thread 0: the candidate plane of output step d (stage D's centre values).
@@ -161,7 +198,7 @@ __global__ void __launch_bounds__(512, 1)
         const int oz = pass / C::K - M, oy = pass % C::K - M;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&barD[b], C::CAND_TX);
-        tma_load_3d(dbuf(b), &mapC, X0 - 4, Y0 + M + oy, Z0 + q + C::H + oz, &barD[b]);
+        tma_load_3d(dbuf(b), &mapC, X0 - 4 - C::CB, Y0 + M + oy, Z0 + q + C::H + oz, &barD[b]);
     };
 
     if (tid == 0) {
@@ -187,9 +224,10 @@ __global__ void __launch_bounds__(512, 1)
         const long long szn = (long long)C::K * C::HY * C::PSZ, sxn = (long long)C::K * C::HY * C::PSX;
         if (hasA) {
             const int g = C::G0 + gi;
-            hasA = range_ok(a.errword, ya * C::BWR + 4 * gi, ya * C::BWR + 4 * gi + 3, C::REF_TX / 4) &&
-                   range_ok(a.errword, ya * C::BWC + 4 * (g - C::R),
-                            ya * C::BWC + 4 * (g + C::R) + 3, C::CAND_TX / 4) &&
+            hasA = range_ok(a.errword, ya * C::BWR + 4 * gi + C::RO,
+                            ya * C::BWR + 4 * gi + C::RO + 3, C::REF_TX / C::ES) &&
+                   range_ok(a.errword, ya * C::BWC + 4 * (g - C::R) + C::CB,
+                            ya * C::BWC + 4 * (g + C::R) + C::CB + 3, C::CAND_TX / C::ES) &&
                    range_ok(a.errword, ya * C::PSZ + 4 * gi,
                             ((C::K - 1) * C::HY + ya) * C::PSZ + 4 * gi + 3, szn);
         }
@@ -208,8 +246,8 @@ __global__ void __launch_bounds__(512, 1)
         }
         const int y = tid >> 5, j = tid & 31;
         okD = range_ok(a.errword, y * C::PSX + j, ((C::K - 1) * C::HY + y) * C::PSX + j, sxn) &&
-              range_ok(a.errword, (N + y) * C::BWC + 4 + N + j,
-                       (N + y) * C::BWC + 4 + N + j + C::K - 1, C::CAND_TX / 4);
+              range_ok(a.errword, (N + y) * C::BWC + 4 + N + j + C::CB,
+                       (N + y) * C::BWC + 4 + N + j + C::CB + C::K - 1, C::CAND_TX / C::ES);
     }
     float Sz[C::K][4];
 
@@ -231,7 +269,13 @@ __global__ void __launch_bounds__(512, 1)
         const bool vin = out_step && vx < a.X && vyy < a.Y;
         const size_t vo = ((size_t)vz * a.Y + vyy) * a.X + vx;
         float2 prev = make_float2(0.f, 0.f);
-        if (vin && pass > 0) prev = acc[vo];
+        float4 prevk = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (vin && pass > 0) {
+            if constexpr (C::KAHAN)
+                prevk = acck[vo];
+            else
+                prev = acc[vo];
+        }
         const int b = t & 1;
         const bool okA = mbar_wait_bounded(&barA[b], (t >> 1) & 1);
         if (!okA) {
@@ -239,27 +283,26 @@ __global__ void __launch_bounds__(512, 1)
             s_abort = 1;
         }
         if (okA && hasA) {
-            const float* ref0 = reinterpret_cast<const float*>(abuf(b));
-            const float* ref1 = ref0 + C::REF_SLOT / 4;
-            const float* cand0 = ref0 + 2 * C::REF_SLOT / 4;
-            const float* cand1 = cand0 + C::CAND_SLOT / 4;
+            const Elem* ref0 = reinterpret_cast<const Elem*>(abuf(b)) + C::RO;
+            const Elem* ref1 = ref0 + C::REF_SLOT / C::ES;
+            const Elem* cand0 = reinterpret_cast<const Elem*>(abuf(b) + 2 * C::REF_SLOT) + C::CB;
+            const Elem* cand1 = cand0 + C::CAND_SLOT / C::ES;
             const int g = C::G0 + gi;
-            const float4 a0 = *reinterpret_cast<const float4*>(ref0 + ya * C::BWR + 4 * gi);
+            const float4 a0 = load4(ref0 + ya * C::BWR + 4 * gi);
             const float av[4] = {a0.x, a0.y, a0.z, a0.w};
             float c0[4 * (2 * C::R + 1)];
 #pragma unroll
             for (int r = 0; r <= 2 * C::R; ++r)
-                *reinterpret_cast<float4*>(&c0[4 * r]) =
-                    *reinterpret_cast<const float4*>(cand0 + ya * C::BWC + 4 * (g - C::R + r));
+                *reinterpret_cast<float4*>(&c0[4 * r]) = load4(cand0 + ya * C::BWC + 4 * (g - C::R + r));
             if (s != N) {
                 // second plane: added (warm-up) or dropped (leaving)
-                const float4 a1 = *reinterpret_cast<const float4*>(ref1 + ya * C::BWR + 4 * gi);
+                const float4 a1 = load4(ref1 + ya * C::BWR + 4 * gi);
                 const float lv[4] = {a1.x, a1.y, a1.z, a1.w};
                 float c1[4 * (2 * C::R + 1)];
 #pragma unroll
                 for (int r = 0; r <= 2 * C::R; ++r)
                     *reinterpret_cast<float4*>(&c1[4 * r]) =
-                        *reinterpret_cast<const float4*>(cand1 + ya * C::BWC + 4 * (g - C::R + r));
+                        load4(cand1 + ya * C::BWC + 4 * (g - C::R + r));
                 if (s < N) {
 #pragma unroll
                     for (int k = 0; k < C::K; ++k)
@@ -370,21 +413,31 @@ __global__ void __launch_bounds__(512, 1)
                 s_abort = 1;
             } else if (okD) {
                 const int y = vy, j = vj;
-                const float* cpl =
-                    reinterpret_cast<const float*>(dbuf(db)) + (N + y) * C::BWC + 4 + N + j;
+                const Elem* cpl =
+                    reinterpret_cast<const Elem*>(dbuf(db)) + (N + y) * C::BWC + 4 + N + j + C::CB;
                 float zl[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < C::K; ++k) {
                     const float w = ex2_neg(Sxb[(k * C::HY + y) * C::PSX + j]);
                     zl[k & 1] += w;
-                    nl[k & 1] = fmaf(w, cpl[k], nl[k & 1]);
+                    nl[k & 1] = fmaf(w, to_f32(cpl[k]), nl[k & 1]);
                 }
                 if (vin) {
-                    const float zt = prev.x + (zl[0] + zl[1]);
-                    const float nt = prev.y + (nl[0] + nl[1]);
+                    float zt, nt;
+                    float4 nk;
+                    if constexpr (C::KAHAN) {
+                        nk = kahan_step(prevk, zl[0] + zl[1], nl[0] + nl[1]);
+                        zt = nk.x;
+                        nt = nk.y;
+                    } else {
+                        zt = prev.x + (zl[0] + zl[1]);
+                        nt = prev.y + (nl[0] + nl[1]);
+                    }
                     if (pass == P - 1 && a.nsplit == 1) {
                         a.out[vo] = nt / zt * a.inv_scale;
                         if (a.zsum) a.zsum[vo] = zt;
+                    } else if constexpr (C::KAHAN) {
+                        acck[vo] = nk;
                     } else {
                         acc[vo] = make_float2(zt, nt);
                     }
@@ -399,5 +452,101 @@ __global__ void __launch_bounds__(512, 1)
         mbar_wait_bounded(&barD[lastD & 1], (lastD >> 1) & 1);
     }
 }
+
+// out = (num_0 + num_1) / (Z_0 + Z_1) over the voxels [v0, v0 + n) of two
+// accumulator buffers (the two halves of the passes), always added in that order.
+// KAHAN: the buffers hold (Z, num, cZ, cnum) Kahan pairs; each half contributes
+// its sum minus its compensation.
+template <bool KAHAN>
+__global__ void __launch_bounds__(256) lp_combine_kernel(const void* __restrict__ accv,
+                                                         size_t stride, size_t v0, size_t n,
+                                                         float inv_scale, float* __restrict__ out,
+                                                         float* __restrict__ zsum) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t v = v0 + i;
+        float zt, nt;
+        if constexpr (KAHAN) {
+            const float4* acc = static_cast<const float4*>(accv);
+            const float4 h0 = acc[v], h1 = acc[stride + v];
+            zt = (h0.x - h0.z) + (h1.x - h1.z);
+            nt = (h0.y - h0.w) + (h1.y - h1.w);
+        } else {
+            const float2* acc = static_cast<const float2*>(accv);
+            const float2 h0 = acc[v], h1 = acc[stride + v];
+            zt = h0.x + h1.x;
+            nt = h0.y + h1.y;
+        }
+        out[v] = nt / zt * inv_scale;
+        if (zsum) zsum[v] = zt;
+    }
+}
+
+template <int M, int N, typename T>
+inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,
+                          float* out, float* zsum, void* acc, unsigned int* errword,
+                          cudaStream_t stream, int zc0, int zc1) {
+    using C = Lp3d<M, N, T>;
+    if (st.elem != C::ES) return cudaErrorInvalidValue;
+    CUtensorMap mapR, mapC;
+    const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
+    const uint64_t strides[2] = {(uint64_t)st.Xs * C::ES, (uint64_t)st.Xs * st.Yp * C::ES};
+    const uint32_t boxR[3] = {(uint32_t)C::BWR, (uint32_t)C::HY, 1};
+    const uint32_t boxC[3] = {(uint32_t)C::BWC, (uint32_t)C::HY, 1};
+    void* base = const_cast<void*>(staged);
+    cudaError_t e = encode_tensor_map(&mapR, C::ES == 2, 3, dims, strides, boxR, base);
+    if (e == cudaSuccess) e = encode_tensor_map(&mapC, C::ES == 2, 3, dims, strides, boxC, base);
+    if (e != cudaSuccess) return e;
+    auto kern = nlm3d_lp_kernel<M, N, T>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    if (zc1 < 0) zc1 = (st.Z + tz - 1) / tz;
+    if (zc1 <= zc0) return cudaSuccess;
+    const int nsplit = nlm3d_lp_split(st.X, st.Y, st.Z, tz);
+    LpArgs a;
+    a.X = st.X;
+    a.Y = st.Y;
+    a.Z = st.Z;
+    a.TZ = tz;
+    a.zc0 = zc0;
+    a.nzc = zc1 - zc0;
+    a.nsplit = nsplit;
+    a.part_stride = (size_t)st.X * st.Y * st.Z;
+    a.inv_scale = inv_scale;
+    a.acc = acc;
+    a.out = out;
+    a.zsum = zsum;
+    a.errword = errword;
+    dim3 grid((st.X + C::CX - 1) / C::CX, (st.Y + C::CY - 1) / C::CY, (zc1 - zc0) * nsplit);
+    kern<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(mapR, mapC, a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || nsplit == 1) return e;
+    const size_t plane = (size_t)st.X * st.Y;
+    const size_t v0 = (size_t)zc0 * tz * plane;
+    const size_t v1 = (size_t)std::min(zc1 * tz, st.Z) * plane;
+    const size_t blocks = std::min<size_t>((v1 - v0 + 255) / 256, (size_t)device_sm_count() * 8);
+    lp_combine_kernel<C::KAHAN><<<(unsigned)blocks, 256, 0, stream>>>(acc, a.part_stride, v0,
+                                                                      v1 - v0, inv_scale, out,
+                                                                      zsum);
+    return cudaGetLastError();
+}
+
+// Compiled (sr, pr) instances: search radius 1..6 with patch radius 3..8 (the
+// reference's NS 7..17), plus the small-patch pairs the register-brick kernel
+// does not cover.
+#define GNLM_LP3D_CASES(X_)                                                        \
+    X_(1, 3) X_(2, 3) X_(3, 3) X_(4, 3) X_(5, 3) X_(6, 3)                          \
+    X_(1, 4) X_(2, 4) X_(3, 4) X_(4, 4) X_(5, 4) X_(6, 4)                          \
+    X_(1, 5) X_(2, 5) X_(3, 5) X_(4, 5) X_(5, 5) X_(6, 5)                          \
+    X_(1, 6) X_(2, 6) X_(3, 6) X_(4, 6) X_(5, 6) X_(6, 6)                          \
+    X_(1, 7) X_(2, 7) X_(3, 7) X_(4, 7) X_(5, 7) X_(6, 7)                          \
+    X_(1, 8) X_(2, 8) X_(3, 8) X_(4, 8) X_(5, 8) X_(6, 8)                          \
+    X_(6, 1) X_(1, 2) X_(2, 2) X_(4, 2) X_(6, 2)
+
+// FP16-storage launches (nlm3d_lp_h.cu), one explicit instance per compiled pair.
+template <int M, int N>
+cudaError_t launch_lp_h(const Staging& st, const void* staged, int tz, float inv_scale, float* out,
+                        float* zsum, void* acc, unsigned int* errword, cudaStream_t stream,
+                        int zc0, int zc1);
 
 }  // namespace gnlm

@@ -121,10 +121,6 @@ int resolve_ws(void** d_ws, size_t* ws_bytes, size_t need, cudaStream_t stream) 
     return NLM_OK;
 }
 
-// 3D staging: FP32 layout, or the row-pair layout for FP16 storage.
-Staging staging3d(int X, int Y, int Z, int H, bool fp16) {
-    return fp16 ? make_staging_pairs(X, Y, Z, H) : make_staging(X, Y, Z, H, H, false);
-}
 
 float weight_scale(int pr, int dims, float h) {
     const double k = 2.0 * pr + 1.0;
@@ -359,19 +355,17 @@ int nlm_release_cached(void) {
 
 size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags) {
     if (X < 1 || Y < 1 || Z < 1 || sr < 0 || pr < 0) return 0;
-    const int H = sr + pr;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
-    return staging3d(X, Y, Z, H, fp16).bytes() + nlm3d_fwd_extra_bytes(X, Y, Z, sr, pr, fp16);
+    return staging3d(X, Y, Z, sr, pr, fp16).bytes() + nlm3d_fwd_extra_bytes(X, Y, Z, sr, pr, fp16);
 }
 
 static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
                         float h, unsigned int flags, void** d_ws, size_t* ws_bytes,
                         cudaStream_t stream) {
-    const int H = sr + pr;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
     if (!nlm3d_fwd_supported(sr, pr, fp16))
         return fail(NLM_ERR_UNSUPPORTED, "3D (sr=%d, pr=%d) not compiled in", sr, pr);
-    Staging st = staging3d(X, Y, Z, H, fp16);
+    Staging st = staging3d(X, Y, Z, sr, pr, fp16);
     int rc = resolve_ws(d_ws, ws_bytes, nlm3d_workspace_bytes(X, Y, Z, sr, pr, flags), stream);
     if (rc) return rc;
     cudaError_t e = launch_stage(d_in, in_dtype, (flags & NLM_FLAG_PREPADDED) != 0,
@@ -383,9 +377,8 @@ static int stage3d_impl(const void* d_in, int in_dtype, int X, int Y, int Z, int
 static int fwd3d_staged_impl(const void* d_ws, int X, int Y, int Z, int sr, int pr, float h,
                              float* d_out, float* d_zsum, unsigned int flags,
                              cudaStream_t stream) {
-    const int H = sr + pr;
     const bool fp16 = (flags & NLM_FLAG_FP16_STORAGE) != 0;
-    Staging st = staging3d(X, Y, Z, H, fp16);
+    Staging st = staging3d(X, Y, Z, sr, pr, fp16);
     cudaError_t e = launch_nlm3d_fwd(st, d_ws, sr, pr, fp16, tuned_variant(3, sr, pr, fp16),
                                      1.0f / weight_scale(pr, 3, h), d_out, d_zsum,
                                      device_error_word(), stream);
@@ -531,7 +524,7 @@ int nlm_autotune(int dims, int X, int Y, int Z, int sr, int pr, unsigned int fla
     if (rc) return rc;
     const bool ok = dims == 3 ? nlm3d_fwd_supported(sr, pr, fp16) : nlm2d_fwd_supported(sr, pr, fp16);
     if (!ok) return fail(NLM_ERR_UNSUPPORTED, "%dD (sr=%d, pr=%d) not compiled in", dims, sr, pr);
-    const Staging st = dims == 3 ? staging3d(X, Y, Z, sr + pr, fp16)
+    const Staging st = dims == 3 ? staging3d(X, Y, Z, sr, pr, fp16)
                                  : make_staging(X, Y, 1, sr + pr, 0, fp16);
     const size_t nvox = (size_t)X * Y * Z;
     void *d_in = nullptr, *d_ws = nullptr;
@@ -623,7 +616,7 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     if (e == cudaSuccess && !hp->s_d2h) e = cudaStreamCreateWithFlags(&hp->s_d2h, cudaStreamNonBlocking);
     if (e == cudaSuccess && !hp->s_c2) e = cudaStreamCreateWithFlags(&hp->s_c2, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
-    const Staging st = staging3d(X, Y, Z, H, fp16);
+    const Staging st = staging3d(X, Y, Z, sr, pr, fp16);
     const size_t plane_in =
         (prepadded ? (size_t)(X + 2 * H) * (Y + 2 * H) : (size_t)X * Y) * dtype_bytes(in_dtype);
     const int in_planes = prepadded ? Z + 2 * H : Z;

@@ -40,6 +40,9 @@ struct Staging {
 Staging make_staging(int X, int Y, int Z, int H, int Hz, bool fp16);
 // 3D FP16-storage staging (row-pair layout).
 Staging make_staging_pairs(int X, int Y, int Z, int H);
+// The staging layout the 3D forward uses for (sr, pr, fp16): FP32; FP16 row pairs
+// (register-brick kernel); or plain FP16 (large-patch kernel).
+Staging staging3d(int X, int Y, int Z, int sr, int pr, bool fp16);
 
 // Pads, converts and scales `in` into `dst` (layout of `st`).  in_dtype is an
 // nlm_dtype; with `prepadded` the input already has the halo (layout
@@ -54,8 +57,8 @@ cudaError_t launch_stage(const void* in, int in_dtype, bool prepadded, float sca
 // [zt0, zt1): range of z tiles to compute (zt1 < 0: through the last); a z tile
 // is nlm3d_fwd_tile_z(sr, pr, fp16, variant) output planes.
 // Large-patch configurations (nlm3d_fwd_large_patch) keep per-voxel (Z, num)
-// accumulator pairs (two buffers) in the workspace right after the staged volume:
-// nlm3d_fwd_extra_bytes() more bytes at staged + st.bytes().
+// accumulator pairs (two buffers; Kahan pairs with FP16 storage) in the workspace right
+// after the staged volume: nlm3d_fwd_extra_bytes() more bytes at staged + st.bytes().
 cudaError_t launch_nlm3d_fwd(const Staging& st, const void* staged, int sr, int pr, bool fp16,
                              int variant, float inv_scale, float* out, float* zsum,
                              unsigned int* errword, cudaStream_t stream, int zt0 = 0,
@@ -67,11 +70,13 @@ bool nlm3d_fwd_large_patch(int sr, int pr, bool fp16);
 size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16);
 
 // Large-patch kernel (nlm3d_lp.cu): chunk depth per variant, compiled pairs, launch.
+// FP32 staging, or (fp16) plain FP16 staging [Zp][Yp][Xs]; `acc` holds two buffers of
+// per-voxel (Z, num) float2, or (Z, num, cZ, cnum) float4 Kahan pairs for FP16.
 int nlm3d_lp_tile_z(int variant);
 bool nlm3d_lp_supported(int sr, int pr);
 int nlm3d_lp_split(int X, int Y, int Z, int tz);
-cudaError_t launch_nlm3d_lp(const Staging& st, const void* staged, int sr, int pr, int variant,
-                            float inv_scale, float* out, float* zsum, float2* acc,
+cudaError_t launch_nlm3d_lp(const Staging& st, const void* staged, int sr, int pr, bool fp16,
+                            int variant, float inv_scale, float* out, float* zsum, void* acc,
                             unsigned int* errword, cudaStream_t stream, int zc0, int zc1);
 
 // 3D adjoint (see nlm3d_adj.cu).  Scratch: (G, out') pairs (2 st.bytes()), gpad'

@@ -335,13 +335,30 @@ def bench_large_patch(torch, gnlm, reps=3):
     nvox = shape[0] * shape[1] * shape[2]
     pairs = nvox * (2 * sr + 1) ** 3
     gnlm.set_variant(3, sr, pr, -1)
+    g = out.cpu().numpy()
+    # the FP16-storage form of the same configuration
+    best16, tune16 = gnlm.autotune(3, shape, sr, pr, fp16_storage=True)
+    gnlm.nlm3d_forward(x, sr, pr, 0.05, out=out, fp16_storage=True)
+    torch.cuda.synchronize()
+    ms16 = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        gnlm.nlm3d_forward(x, sr, pr, 0.05, out=out, fp16_storage=True)
+        e1.record()
+        e1.synchronize()
+        ms16.append(e0.elapsed_time(e1))
+    t16 = min(ms16)
+    g16 = out.cpu().numpy()
+    gnlm.set_variant(3, sr, pr, -1, fp16_storage=True)
     # FP64 oracle on 16^3 boxes at the 8 corners, the 6 face centres and the centre
     import oracle as O
     blk = (16, 16, 16)
     origins = O.border_blocks(shape, blk)
     ref = O.nlm3d_blocks(v, sr, pr, 0.05, origins, blk)
-    g = out.cpu().numpy()
     d = np.stack([g[z:z + 16, y:y + 16, x:x + 16] for (z, y, x) in origins]).astype(np.float64) - ref
+    d16 = np.stack([g16[z:z + 16, y:y + 16, x:x + 16]
+                    for (z, y, x) in origins]).astype(np.float64) - ref
     return {"shape": list(shape), "search_radius": sr, "patch_radius": pr, "ms": round(t, 3),
             "max_abs_err_vs_fp64": float(np.abs(d).max()),
             "rms_err_vs_fp64": float(np.sqrt(np.mean(d * d))),
@@ -351,6 +368,10 @@ def bench_large_patch(torch, gnlm, reps=3):
             "gpairs_per_s": round(pairs / (t * 1e-3) / 1e9, 1),
             "tflops": round(FLOPS_PER_PAIR * pairs / (t * 1e-3) / 1e12, 2),
             "kernel": "nlm3d_lp_kernel<6,8>", "variant": best,
+            "fp16_storage": {"ms": round(t16, 3), "value": round(nvox / (t16 * 1e-3) / 1e6, 2),
+                             "variant": best16, "autotune_ms": [round(v, 3) for v in tune16],
+                             "max_abs_err_vs_fp64": float(np.abs(d16).max()),
+                             "rms_err_vs_fp64": float(np.sqrt(np.mean(d16 * d16)))},
             "autotune_ms": [round(v, 3) for v in tune]}
 
 

@@ -39,6 +39,9 @@ def run_cases(gnlm, torch):
     xl = torch.from_numpy(vl).cuda()
     for sr, pr in [(6, 8), (2, 4), (6, 1)]:
         res[f"lp_{sr}_{pr}"] = gnlm.nlm3d_forward(xl, sr, pr, 0.05).cpu().numpy()
+    for sr, pr in [(6, 8), (1, 3)]:
+        res[f"lp16_{sr}_{pr}"] = gnlm.nlm3d_forward(xl, sr, pr, 0.05,
+                                                    fp16_storage=True).cpu().numpy()
     im, _ = phantom.disc_rect_phantom((61, 90), n_shapes=6, sigma=0.08, seed=5)
     x2 = torch.from_numpy(im).cuda()
     for var in range(gnlm.variant_count(2, False)):
