@@ -98,9 +98,10 @@ int nlm_release_cached(void);
 
 /* Bytes of scratch nlm3d_forward needs for this shape (0 on invalid input).
  * Compiled (sr, pr): sr 1..5 with pr 1, sr 3 and 5 with pr 2 (register-brick
- * kernel, FP32 or FP16 storage), and sr 1..6 with pr 1..8 otherwise
- * (large-patch kernel, FP32 only: the reference's NS 7..17 configurations);
- * for the latter the scratch also holds two (Z, num) float pairs per voxel. */
+ * kernel), and sr 1..6 with pr 1..8 otherwise (large-patch kernel: the
+ * reference's NS 7..17 configurations), each in FP32 or FP16 storage; for the
+ * latter kernel the scratch also holds two (Z, num) float pairs per voxel, or two
+ * (Z, num, cZ, cnum) Kahan pairs with FP16 storage. */
 size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags);
 
 /*
@@ -135,13 +136,17 @@ int nlm3d_forward_staged(const void* d_ws, size_t ws_bytes, int X, int Y, int Z,
  * application owns all GPU memory through its own pool, and fixed-budget real-time
  * pipelines that reserve everything at start-up, where a cudaMalloc can fail
  * mid-run and a cudaFree stalls the whole device.  The staging scratch is a 16 MiB
- * array compiled into libgnlm.so, held on every GPU that loads the library until
- * the process exits.  Volumes whose staged copy needs more (sr 3, pr 1: beyond 152^3,
- * FP32 or FP16 storage) return NLM_ERR_WORKSPACE.  The first
- * call on each device looks up the array's device address (make that first call
- * before any stream capture).  All calls on a device share the array: calls whose
- * GPU work overlaps race, so serialise them (e.g. on one stream).  The array keeps
- * the last call's contents; nothing in it needs to start at zero.
+ * array compiled into libgnlm.so: a GPU reserves it when the library's module is
+ * loaded there (with CUDA's default lazy loading, at the latest on the first call
+ * of this entry point) and holds it until the process exits.  Arguments are checked
+ * as nlm3d_forward checks them; then volumes whose staged copy needs more (sr 3,
+ * pr 1: beyond 152^3, FP32 or FP16 storage) return NLM_ERR_WORKSPACE.  The first
+ * call in each CUDA context looks up the array's device address (a device reset
+ * makes a new context and a new lookup); make that first call before any stream
+ * capture, since it may also load the module.  All calls on a device share the
+ * array: calls whose GPU work overlaps race, so serialise them (e.g. on one
+ * stream).  The array keeps the last call's contents; nothing in it needs to start
+ * at zero.
  */
 int nlm3d_forward_noalloc(const void* d_in, int in_dtype, int X, int Y, int Z, int sr, int pr,
                           float h, float* d_out, float* d_zsum, unsigned int flags,
