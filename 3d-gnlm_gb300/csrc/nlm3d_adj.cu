@@ -253,18 +253,35 @@ __global__ void __launch_bounds__(32 * NW, 1)
                 float zrow[C::RT][PD];
 #pragma unroll
                 for (int rp = 0; rp < RTP; ++rp) {
-                    float2 run = __fmul2_rn(t2[rp][0], t2[rp][0]);
+                    if constexpr (N == 1 && PD % 2 == 0) {
+                        // three planes' squares summed directly; pairs of output planes
+                        // share their middle pair (no running sum to subtract from)
+                        float2 sq[C::PT];
 #pragma unroll
-                    for (int k = 1; k < K; ++k) run = __ffma2_rn(t2[rp][k], t2[rp][k], run);
-                    zrow[2 * rp][0] = run.x;
-                    zrow[2 * rp + 1][0] = run.y;
+                        for (int p = 0; p < C::PT; ++p) sq[p] = __fmul2_rn(t2[rp][p], t2[rp][p]);
 #pragma unroll
-                    for (int p = 1; p < PD; ++p) {
-                        const float2 tn = t2[rp][p + K - 1], to = t2[rp][p - 1];
-                        run = __ffma2_rn(tn, tn, run);
-                        run = __ffma2_rn(make_float2(-to.x, -to.y), to, run);
-                        zrow[2 * rp][p] = run.x;
-                        zrow[2 * rp + 1][p] = run.y;
+                        for (int p = 0; p < PD; p += 2) {
+                            const float2 m2 = __fadd2_rn(sq[p + 1], sq[p + 2]);
+                            const float2 z0 = __fadd2_rn(sq[p], m2), z1 = __fadd2_rn(m2, sq[p + 3]);
+                            zrow[2 * rp][p] = z0.x;
+                            zrow[2 * rp + 1][p] = z0.y;
+                            zrow[2 * rp][p + 1] = z1.x;
+                            zrow[2 * rp + 1][p + 1] = z1.y;
+                        }
+                    } else {
+                        float2 run = __fmul2_rn(t2[rp][0], t2[rp][0]);
+#pragma unroll
+                        for (int k = 1; k < K; ++k) run = __ffma2_rn(t2[rp][k], t2[rp][k], run);
+                        zrow[2 * rp][0] = run.x;
+                        zrow[2 * rp + 1][0] = run.y;
+#pragma unroll
+                        for (int p = 1; p < PD; ++p) {
+                            const float2 tn = t2[rp][p + K - 1], to = t2[rp][p - 1];
+                            run = __ffma2_rn(tn, tn, run);
+                            run = __ffma2_rn(make_float2(-to.x, -to.y), to, run);
+                            zrow[2 * rp][p] = run.x;
+                            zrow[2 * rp + 1][p] = run.y;
+                        }
                     }
                 }
                 float D[RD][PD];
