@@ -299,9 +299,8 @@ def test_autotune_records_a_variant(torch_cuda, gnlm_lib):
 
 def test_3d_default_tile_shape(torch_cuda, gnlm_lib):
     """With no recorded variant a patch-3 forward runs on the 4 x 6 tiles (variant 5),
-    the fastest shape measured from 64^3 to 256^3.  The 4 x 8 tiles slide their z
-    windows from other planes, so their bits differ and the default's output shows
-    which shape ran; both agree within the FP32 bar."""
+    the fastest shape measured from 64^3 to 192^3.  Where the 4 x 8 tiles give other
+    bits, the default's output shows which shape ran; both agree within the FP32 bar."""
     torch = torch_cuda
     try:
         v, _ = phantom.ellipsoid_phantom((64, 64, 64), n_ellipsoids=8, sigma=0.05, seed=31)
