@@ -15,8 +15,8 @@
 // The persistent kernel runs (occupancy x SMs) CTAs; each CTA takes the next work
 // item with one atomicAdd (no waiting: an index past the end means done), loads the
 // item's tile with TMA on its mbarrier (the phase flips per item) and runs the
-// single-volume kernel's tile body with z offsets in groups of three
-// (fwd3d_tile_pz in nlm3d_tile.cuh).  The tile shape is a template
+// single-volume kernel's tile body with z offsets in groups of four
+// (fwd3d_tile_pz in nlm3d_tile.cuh; 2M+1 = 7 splits 4 + 3, 11 splits 4 + 4 + 3).  The tile shape is a template
 // parameter; the plan's autotuner times each shape on the batch and keeps the
 // fastest.
 #include <stdio.h>
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         switch (v->sr) {
 #define X_(m)                                                                                     \
     case m:                                                                                       \
-        ok = fwd3d_tile_pz<m, 1, RY, RZ, NW, 3>(&v->map, tile, bar, k & 1u, item.y, item.z,      \
+        ok = fwd3d_tile_pz<m, 1, RY, RZ, NW, 4>(&v->map, tile, bar, k & 1u, item.y, item.z,      \
                                                  item.w, v->X, v->Y, v->Z, v->inv_scale, v->out,   \
                                                  v->zsum, errword);                                \
         break;

@@ -144,9 +144,10 @@ static cudaError_t run_fwd3d(const Staging& st, const void* staged, float inv_sc
 //   1: 4 x 8, reference values re-read from shared memory, 3 CTAs/SM
 //   2: 4 x 4, registers, 3 CTAs/SM
 //   3: 2 x 8, registers, 3 CTAs/SM
-//   4: 4 x 8, registers, z offsets in pairs sharing candidate planes, 2 CTAs/SM
-//   5: 4 x 6, z offsets in groups of three, 2 CTAs/SM
-//   6: 4 x 8, groups of three, 2 CTAs/SM
+//   4: 4 x 6, z offsets in groups of four sharing candidate planes (the 2M+1 z offsets
+//      split as 4 + 3 for search 7), 2 CTAs/SM
+//   5: 4 x 6, groups of three (3 + 3 + 1 for search 7), 2 CTAs/SM
+//   6: 4 x 8, groups of four, 2 CTAs/SM
 // FP16-storage form (row-pair layout, Kahan-compensated weight sum):
 //   0: 4 x 6, 2 CTAs/SM;  1: 4 x 8, 2 CTAs/SM;  2: 2 x 8, 3 CTAs/SM
 template <int m, int n>
@@ -159,9 +160,9 @@ static cudaError_t run_variant(const Staging& st, const void* staged, bool fp16,
             case 1: return run_fwd3d<m, n, float, 4, 8, 4, 3, false, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 2: return run_fwd3d<m, n, float, 4, 4, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 3: return run_fwd3d<m, n, float, 2, 8, 4, 3, true, false>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
-            case 4: return run_fwd3d_pz<m, n, 4, 8, 4, 2, 2>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 4: return run_fwd3d_pz<m, n, 4, 6, 4, 2, 4>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
             case 5: return run_fwd3d_pz<m, n, 4, 6, 4, 2, 3>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
-            case 6: return run_fwd3d_pz<m, n, 4, 8, 4, 2, 3>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
+            case 6: return run_fwd3d_pz<m, n, 4, 8, 4, 2, 4>(st, staged, inv_scale, out, zsum, ew, s, zt0, zt1);
         }
     } else {
         switch (v) {
@@ -206,7 +207,7 @@ Staging staging3d(int X, int Y, int Z, int sr, int pr, bool fp16) {
 }
 
 int nlm3d_fwd_tile_z(int sr, int pr, bool fp16, int v) {
-    static const int f32[7] = {8, 8, 4, 8, 8, 6, 8}, f16[3] = {6, 8, 8};
+    static const int f32[7] = {8, 8, 4, 8, 6, 6, 8}, f16[3] = {6, 8, 8};
     if (v < 0 || v >= nlm3d_fwd_variant_count(fp16)) return 0;
     if (nlm3d_fwd_large_patch(sr, pr, fp16)) return nlm3d_lp_tile_z(v);
     return fp16 ? f16[v] : f32[v];

@@ -222,15 +222,15 @@ void* symbol_address(const void* symbol) {
 }
 
 // Variant used before any autotuning: the fastest measured on a GB300 for the
-// configuration family (3D FP32 patch 3: z offsets in groups of three, 4 x 6 tiles,
-// faster than 4 x 8 up to 192^3 and 2.8 % slower at 256^3, where the autotuner picks
-// 4 x 8; search 11 / patch 5: groups of three, 4 x 6;
-// 2D FP32: two columns per lane, 8 rows x 4 warps), else variant 0.
+// configuration family (3D FP32 patch 3: z offsets in groups of four, 4 x 6 tiles,
+// fastest from 128^3 to 256^3; search 11 / patch 5: groups of three, 4 x 6, whose
+// groups of four spill registers; 2D FP32: two columns per lane, 8 rows x 4 warps),
+// else variant 0.
 int default_variant(int dims, int sr, int pr, bool fp16) {
     if (fp16) return 0;
     if (dims == 3) {
         if (nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
-        if (pr == 1) return 5;
+        if (pr == 1) return 4;
         if (pr == 2 && sr == 5) return 5;
         return 0;
     }

@@ -147,7 +147,7 @@ def test_default_variants_without_autotune(L):
     """Before any autotuning the forward uses the measured per-configuration default
     (no GPU needed to read it)."""
     fp16 = gnlm.NLM_FLAG_FP16_STORAGE
-    assert L.nlm_get_variant(3, 3, 1, 0) == 5   # 3D FP32 patch 3: z offsets in groups of three, 4 x 6
+    assert L.nlm_get_variant(3, 3, 1, 0) == 4   # 3D FP32 patch 3: z offsets in groups of four, 4 x 6
     assert L.nlm_get_variant(3, 5, 2, 0) == 5
     assert L.nlm_get_variant(3, 3, 2, 0) == 0
     assert L.nlm_get_variant(3, 3, 1, fp16) == 0
