@@ -464,7 +464,7 @@ static cudaError_t run2d_variant(const Staging& st, const void* staged, bool fp1
             case 2: return run_fwd2d<m, n, float, 16, 8, 2>(st, staged, inv_scale, out, zsum, ew, s);
             case 3: return run_fwd2d<m, n, float, 16, 4, 3, 3>(st, staged, inv_scale, out, zsum, ew, s);
             case 4: return run_fwd2d<m, n, float, 16, 8, 2, 3>(st, staged, inv_scale, out, zsum, ew, s);
-            case 5: return run_fwd2d_c2<m, n, 8, 4, 3, 3>(st, staged, inv_scale, out, zsum, ew, s);
+            case 5: return run_fwd2d_c2<m, n, 8, 4, 3, 6>(st, staged, inv_scale, out, zsum, ew, s);
             case 6: return run_fwd2d_c2<m, n, 4, 8, 2, 3>(st, staged, inv_scale, out, zsum, ew, s);
         }
     }
