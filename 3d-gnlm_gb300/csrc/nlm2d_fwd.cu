@@ -441,8 +441,8 @@ static cudaError_t run_fwd2d(const Staging& st, const void* staged, float inv_sc
 
 // Tile variants: 0: 16 rows per thread, 4 warps; 1: 8 rows, 4 warps; 2: 16 rows, 8 warps;
 // 3, 4: as 0 and 2 with y offsets in groups of three; 5, 6: two columns per lane
-// (nlm2d_fwd_c2_kernel) with 8 rows x 4 warps and 4 rows x 8 warps (FP32; FP16 storage
-// runs variant 4 for them).
+// (nlm2d_fwd_c2_kernel) with 8 rows x 4 warps in groups of six and 4 rows x 8 warps in
+// groups of three (FP32; FP16 storage runs variant 4 for them).
 template <int m, int n>
 static cudaError_t run2d_variant(const Staging& st, const void* staged, bool fp16, int v,
                                  float inv_scale, float* out, float* zsum, unsigned int* ew,
