@@ -81,12 +81,14 @@ struct Lp3d {
     static constexpr int CAND_TX = BWC * HY * ES;  // bytes of a candidate plane box
     static constexpr int REF_SLOT = cround(REF_TX, 128);
     static constexpr int CAND_SLOT = cround(CAND_TX, 128);
+    static constexpr int DC_TX = BWC * CY * ES;    // bytes of a stage-D candidate box (CY rows)
+    static constexpr int DC_SLOT = cround(DC_TX, 128);
     static constexpr int ABUF = 2 * REF_SLOT + 2 * CAND_SLOT;  // entering/leaving ref + cand
     static constexpr int SZ_OFF = 0;
     static constexpr int SX_OFF = SZ_OFF + cround(K * HY * PSZ * 4, 128);
     static constexpr int A_OFF = SX_OFF + cround(K * HY * PSX * 4, 128);
     static constexpr int D_OFF = A_OFF + 2 * ABUF;
-    static constexpr int BAR_OFF = D_OFF + 2 * CAND_SLOT;
+    static constexpr int BAR_OFF = D_OFF + 2 * DC_SLOT;
     static constexpr int SMEM_BYTES = BAR_OFF + 64;
     static_assert(M >= 1 && N >= 1, "radii");
     static_assert(NG <= 16 && NA <= THREADS && NB <= THREADS && NC <= THREADS,
@@ -136,7 +138,8 @@ __device__ __forceinline__ float4 kahan_step(float4 acc, float dz, float dn) {
 template <int M, int N, typename Elem>
 __global__ void __launch_bounds__(512, 1)
     nlm3d_lp_kernel(const __grid_constant__ CUtensorMap mapR,
-                    const __grid_constant__ CUtensorMap mapC, const LpArgs a) {
+                    const __grid_constant__ CUtensorMap mapC,
+                    const __grid_constant__ CUtensorMap mapD, const LpArgs a) {
     using C = Lp3d<M, N, Elem>;
     extern __shared__ __align__(128) unsigned char smem[];
     float* Szb = reinterpret_cast<float*>(smem + C::SZ_OFF);
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(512, 1)
     const int TD = P * TZc;     // output steps
 
     auto abuf = [&](int b) { return smem + C::A_OFF + b * C::ABUF; };
-    auto dbuf = [&](int b) { return smem + C::D_OFF + b * C::CAND_SLOT; };
+    auto dbuf = [&](int b) { return smem + C::D_OFF + b * C::DC_SLOT; };
 
     // Thread 0: loads of step t's planes into A buffer t&1 (slot 0: the entering
     // plane, slot 1: the second warm-up plane or the leaving plane).
@@ -192,13 +195,14 @@ __global__ void __launch_bounds__(512, 1)
                         p1 + oz, &barA[b]);
         }
     };
-    // Thread 0: the candidate plane of output step d (stage D's centre values).
+    // Thread 0: the candidate plane of output step d (stage D's centre values: the CY
+    // output rows only, shifted by oy).
     auto issueD = [&](int d) {
         const int b = d & 1, lp = d / TZc, q = d - lp * TZc, pass = pb + lp;
         const int oz = pass / C::K - M, oy = pass % C::K - M;
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&barD[b], C::CAND_TX);
-        tma_load_3d(dbuf(b), &mapC, X0 - 4 - C::CB, Y0 + M + oy, Z0 + q + C::H + oz, &barD[b]);
+        mbar_arrive_expect_tx(&barD[b], C::DC_TX);
+        tma_load_3d(dbuf(b), &mapD, X0 - 4 - C::CB, Y0 + C::H + oy, Z0 + q + C::H + oz, &barD[b]);
     };
 
     if (tid == 0) {
@@ -219,6 +223,8 @@ __global__ void __launch_bounds__(512, 1)
     bool hasA = gi < C::NG && ya < C::HY;
     // Stages B-D own fixed items too; a thread whose ranges leave their buffers
     // (possible only through a defect, caught by NLM_BOUNDS_CHECK builds) skips its work.
+    // Items fill whole warps (shared-memory wavefronts are counted per warp access, so
+    // spreading them over more, partly filled warps costs bandwidth).
     bool okB = tid < C::NB, okC = tid < C::NC, okD = true;
     if constexpr (kBoundsCheck) {
         const long long szn = (long long)C::K * C::HY * C::PSZ, sxn = (long long)C::K * C::HY * C::PSX;
@@ -246,8 +252,8 @@ __global__ void __launch_bounds__(512, 1)
         }
         const int y = tid >> 5, j = tid & 31;
         okD = range_ok(a.errword, y * C::PSX + j, ((C::K - 1) * C::HY + y) * C::PSX + j, sxn) &&
-              range_ok(a.errword, (N + y) * C::BWC + 4 + N + j + C::CB,
-                       (N + y) * C::BWC + 4 + N + j + C::CB + C::K - 1, C::CAND_TX / C::ES);
+              range_ok(a.errword, y * C::BWC + 4 + N + j + C::CB,
+                       y * C::BWC + 4 + N + j + C::CB + C::K - 1, C::DC_TX / C::ES);
     }
     float Sz[C::K][4];
 
@@ -414,7 +420,7 @@ __global__ void __launch_bounds__(512, 1)
             } else if (okD) {
                 const int y = vy, j = vj;
                 const Elem* cpl =
-                    reinterpret_cast<const Elem*>(dbuf(db)) + (N + y) * C::BWC + 4 + N + j + C::CB;
+                    reinterpret_cast<const Elem*>(dbuf(db)) + y * C::BWC + 4 + N + j + C::CB;
                 float zl[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < C::K; ++k) {
@@ -453,34 +459,413 @@ __global__ void __launch_bounds__(512, 1)
     }
 }
 
-// out = (num_0 + num_1) / (Z_0 + Z_1) over the voxels [v0, v0 + n) of two
-// accumulator buffers (the two halves of the passes), always added in that order.
-// KAHAN: the buffers hold (Z, num, cZ, cnum) Kahan pairs; each half contributes
-// its sum minus its compensation.
+// Two CTAs per SM: the x-offset halves.  With one 512-thread CTA per SM every stage
+// boundary is a barrier of the whole SM, and the stages (A: FMA and shared loads, B and
+// C: shared memory, D: ex2) cannot overlap.  This form gives each CTA half of a pass's
+// x offsets (half 0: ox = -M..0, half 1: ox = 1..M) of the same column tile and chunk,
+// in 256 threads and under half the shared memory, so two CTAs share an SM and one runs
+// its stages while the other waits at a barrier.  Stage B writes its x sums in place
+// over the Sz row it read (no separate Sx buffer), the candidate plane boxes cover only
+// the half's window, and every CTA accumulates into its own (Z, num) buffer: part
+// 2 * (pass half) + (x half), added in that order by lp_combine_kernel.
+template <int M, int N, typename T>
+struct Lpx3d {
+    using G = Lp3d<M, N, T>;
+    static constexpr int ES = G::ES, EA = G::EA, K = G::K, CX = G::CX, CY = G::CY, H = G::H;
+    static constexpr int HX = G::HX, HY = G::HY, R = G::R, G0 = G::G0, NG = G::NG, MA = G::MA;
+    static constexpr int PSZ = G::PSZ, BWR = G::BWR, RO = G::RO, BWC = G::BWC, CB = G::CB;
+    static constexpr bool KAHAN = G::KAHAN;
+    static constexpr int KH = M + 1;           // x offsets of half 0 (half 1 has M)
+    static constexpr int THREADS = 256;
+    static constexpr int WG = NG + R;          // 4-column groups of a half's candidate box
+    // Half h's candidate box starts at layout group h ? G0 : G0 - R; FP16 boxes start on a
+    // 16-byte (8-element) boundary, 4 elements early when that group is even.
+    static constexpr int CB0 = ES == 2 && (G0 - R) % 2 == 0 ? 4 : 0;
+    static constexpr int CB1 = ES == 2 && G0 % 2 == 0 ? 4 : 0;
+    static constexpr int BWH = cround(4 * WG + (ES == 2 ? 4 : 0), EA);  // half box width
+    static constexpr int REF_TX = BWR * HY * ES;
+    static constexpr int CAND_TX = BWH * HY * ES;
+    static constexpr int REF_SLOT = cround(REF_TX, 128);
+    static constexpr int CAND_SLOT = cround(CAND_TX, 128);
+    static constexpr int DC_TX = BWC * CY * ES;  // stage-D candidates: the full window
+    static constexpr int DC_SLOT = cround(DC_TX, 128);
+    static constexpr int ABUF = 2 * REF_SLOT + 2 * CAND_SLOT;
+    static constexpr int SZ_OFF = 0;
+    static constexpr int A_OFF = cround(KH * HY * PSZ * 4, 128);
+    static constexpr int D_OFF = A_OFF + 2 * ABUF;
+    static constexpr int BAR_OFF = D_OFF + 2 * DC_SLOT;
+    static constexpr int SMEM_BYTES = BAR_OFF + 64;
+    static_assert(HY <= 32, "stage A: two halo rows per thread");
+    static_assert(KH * HY <= THREADS && KH * CX <= THREADS, "one stage B / C item per thread");
+    static_assert(CX * CY == 2 * THREADS, "two stage-D voxels per thread");
+    static_assert(4 * WG + CB0 <= BWH && 4 * WG + CB1 <= BWH, "half box");
+    static_assert(BWH <= 256 && (BWH * ES) % 16 == 0, "TMA box");
+    static_assert(SMEM_BYTES + 1024 <= 114 * 1024, "two CTAs per SM");
+};
+
+template <int M, int N, typename Elem, int HALF>
+__device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensorMap* mapC,
+                                         const CUtensorMap* mapD, const LpArgs& a,
+                                         unsigned char* smem, int chunk, int part) {
+    using C = Lpx3d<M, N, Elem>;
+    constexpr int KL = HALF ? M : M + 1;          // x offsets of this half
+    constexpr int KB = HALF ? M + 1 : 0;          // ox + M of the half's first x offset
+    constexpr int OG = HALF ? C::G0 : C::G0 - C::R;  // candidate box origin (layout group)
+    constexpr int CBh = HALF ? C::CB1 : C::CB0;
+    constexpr int IB = HALF ? 1 : 4 * C::R - M;   // window index of (column 0, offset 0)
+    float* Szb = reinterpret_cast<float*>(smem + C::SZ_OFF);
+    uint64_t* barA = reinterpret_cast<uint64_t*>(smem + C::BAR_OFF);
+    uint64_t* barD = barA + 2;
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x;
+    const int X0 = blockIdx.x * C::CX, Y0 = blockIdx.y * C::CY;
+    const int Z0 = (chunk + a.zc0) * a.TZ;
+    const int TZc = min(a.TZ, a.Z - Z0);
+    if (TZc <= 0) return;  // uniform over the CTA
+    const int sp = part >> 1;  // pass half
+    const int pb = sp * (C::K * C::K) / a.nsplit;
+    const int P = (sp + 1) * (C::K * C::K) / a.nsplit - pb;
+    float2* const acc = static_cast<float2*>(a.acc) + part * a.part_stride;
+    float4* const acck = static_cast<float4*>(a.acc) + part * a.part_stride;
+    const int SPP = N + TZc;
+    const int T = P * SPP;
+    const int TD = P * TZc;
+
+    auto abuf = [&](int b) { return smem + C::A_OFF + b * C::ABUF; };
+    auto dbuf = [&](int b) { return smem + C::D_OFF + b * C::DC_SLOT; };
+    // Thread 0: loads of step t's planes (as in nlm3d_lp_kernel; candidates: the half's box).
+    auto issueA = [&](int t) {
+        const int b = t & 1, lp = t / SPP, s = t - lp * SPP, pass = pb + lp;
+        const int oz = pass / C::K - M, oy = pass % C::K - M;
+        int p0, p1 = -1;
+        if (s < N) {
+            p0 = Z0 + M + 2 * s;
+            p1 = p0 + 1;
+        } else {
+            const int q = s - N;
+            p0 = Z0 + M + 2 * N + q;
+            if (q >= 1) p1 = Z0 + M + q - 1;
+        }
+        unsigned char* base = abuf(b);
+        const int xr = X0 - 4 + 4 * C::G0, yr = Y0 + M, xc = X0 - 4 + 4 * OG - CBh;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&barA[b], (p1 >= 0 ? 2u : 1u) * (C::REF_TX + C::CAND_TX));
+        tma_load_3d(base, mapR, xr - C::RO, yr, p0, &barA[b]);
+        tma_load_3d(base + 2 * C::REF_SLOT, mapC, xc, yr + oy, p0 + oz, &barA[b]);
+        if (p1 >= 0) {
+            tma_load_3d(base + C::REF_SLOT, mapR, xr - C::RO, yr, p1, &barA[b]);
+            tma_load_3d(base + 2 * C::REF_SLOT + C::CAND_SLOT, mapC, xc, yr + oy, p1 + oz,
+                        &barA[b]);
+        }
+    };
+    // Thread 0: stage D's candidate plane of output step d (CY rows, full x window).
+    auto issueD = [&](int d) {
+        const int b = d & 1, lp = d / TZc, q = d - lp * TZc, pass = pb + lp;
+        const int oz = pass / C::K - M, oy = pass % C::K - M;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&barD[b], C::DC_TX);
+        tma_load_3d(dbuf(b), mapD, X0 - 4 - C::CB, Y0 + C::H + oy, Z0 + q + C::H + oz, &barD[b]);
+    };
+
+    if (tid == 0) {
+        for (int i = 0; i < 4; ++i) mbar_init(&barA[i], 1);
+        fence_mbar_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+    int lastA = 0, lastD = 0;
+    if (tid == 0) {
+        issueA(0);
+        issueD(0);
+    }
+
+    // Stage A: 16 lanes per halo row, lane gi < NG owns columns 4*(G0+gi) .. +3 of rows
+    // ya0 and ya0 + 16.
+    const int gi = tid & 15, ya0 = tid >> 4;
+    bool hasA[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) hasA[r] = gi < C::NG && ya0 + 16 * r < C::HY;
+    bool okB = tid < KL * C::HY, okC = tid < KL * C::CX, okD = true;
+    if constexpr (kBoundsCheck) {
+        const long long szn = (long long)KL * C::HY * C::PSZ;
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+            if (hasA[r]) {
+                const int ya = ya0 + 16 * r;
+                hasA[r] = range_ok(a.errword, ya * C::BWR + 4 * gi + C::RO,
+                                   ya * C::BWR + 4 * gi + C::RO + 3, C::REF_TX / C::ES) &&
+                          range_ok(a.errword, ya * C::BWH + 4 * gi + CBh,
+                                   ya * C::BWH + 4 * (gi + C::R) + CBh + 3, C::CAND_TX / C::ES) &&
+                          range_ok(a.errword, ya * C::PSZ + 4 * gi,
+                                   ((KL - 1) * C::HY + ya) * C::PSZ + 4 * gi + 3, szn);
+            }
+        if (okB) {
+            constexpr int NV = (C::MA + C::HX + 3) / 4;
+            okB = range_ok(a.errword, tid * C::PSZ, tid * C::PSZ + 4 * NV - 1, szn);
+        }
+        if (okC) {
+            const int k = tid >> 5, j = tid & 31;
+            okC = range_ok(a.errword, k * C::HY * C::PSZ + j,
+                           k * C::HY * C::PSZ + j + (C::HY - 1) * C::PSZ, szn);
+        }
+        const int y = tid >> 5, j = tid & 31;
+        okD = range_ok(a.errword, y * C::PSZ + j, ((KL - 1) * C::HY + y + 8) * C::PSZ + j, szn) &&
+              range_ok(a.errword, y * C::BWC + 4 + N + j + C::CB + KB,
+                       (y + 8) * C::BWC + 4 + N + j + C::CB + KB + KL - 1, C::DC_TX / C::ES);
+    }
+    float Sz[2][KL][4];
+
+    int d = 0;
+    for (int t = 0; t < T; ++t) {
+        const int pass = t / SPP, s = t - pass * SPP;
+        if (tid == 0 && t + 1 < T) issueA(lastA = t + 1);
+        if (s == 0) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+#pragma unroll
+                for (int k = 0; k < KL; ++k)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) Sz[r][k][c] = 0.f;
+        }
+        const bool out_step = s >= N;
+        // the two voxels' sums from earlier passes, requested early
+        const int vy = tid >> 5, vj = tid & 31;
+        const int vx = X0 + vj, vz = Z0 + (s - N);
+        size_t vo[2];
+        bool vin[2];
+        float2 prev[2];
+        float4 prevk[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int vyy = Y0 + vy + 8 * u;
+            vin[u] = out_step && vx < a.X && vyy < a.Y;
+            vo[u] = ((size_t)vz * a.Y + vyy) * a.X + vx;
+            prev[u] = make_float2(0.f, 0.f);
+            prevk[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (vin[u] && pass > 0) {
+                if constexpr (C::KAHAN)
+                    prevk[u] = acck[vo[u]];
+                else
+                    prev[u] = acc[vo[u]];
+            }
+        }
+        const int b = t & 1;
+        const bool okA = mbar_wait_bounded(&barA[b], (t >> 1) & 1);
+        if (!okA) {
+            raise_device_error(a.errword, DEVERR_TMA_TIMEOUT);
+            s_abort = 1;
+        }
+        if (okA) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                if (!hasA[r]) continue;
+                const int ya = ya0 + 16 * r;
+                const Elem* ref0 = reinterpret_cast<const Elem*>(abuf(b)) + C::RO;
+                const Elem* ref1 = ref0 + C::REF_SLOT / C::ES;
+                const Elem* cand0 = reinterpret_cast<const Elem*>(abuf(b) + 2 * C::REF_SLOT) + CBh;
+                const Elem* cand1 = cand0 + C::CAND_SLOT / C::ES;
+                const float4 a0 = load4(ref0 + ya * C::BWR + 4 * gi);
+                const float av[4] = {a0.x, a0.y, a0.z, a0.w};
+                float c0[4 * (C::R + 1)];
+#pragma unroll
+                for (int w = 0; w <= C::R; ++w)
+                    *reinterpret_cast<float4*>(&c0[4 * w]) = load4(cand0 + ya * C::BWH + 4 * (gi + w));
+                if (s != N) {
+                    const float4 a1 = load4(ref1 + ya * C::BWR + 4 * gi);
+                    const float lv[4] = {a1.x, a1.y, a1.z, a1.w};
+                    float c1[4 * (C::R + 1)];
+#pragma unroll
+                    for (int w = 0; w <= C::R; ++w)
+                        *reinterpret_cast<float4*>(&c1[4 * w]) =
+                            load4(cand1 + ya * C::BWH + 4 * (gi + w));
+                    if (s < N) {  // warm-up: both planes enter
+#pragma unroll
+                        for (int k = 0; k < KL; ++k)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                const float de = av[c] - c0[IB + c + k];
+                                const float dl = lv[c] - c1[IB + c + k];
+                                Sz[r][k][c] = fmaf(dl, dl, fmaf(de, de, Sz[r][k][c]));
+                            }
+                    } else {  // the second plane leaves
+#pragma unroll
+                        for (int k = 0; k < KL; ++k)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                const float de = av[c] - c0[IB + c + k];
+                                const float dl = lv[c] - c1[IB + c + k];
+                                Sz[r][k][c] = fmaf(-dl, dl, fmaf(de, de, Sz[r][k][c]));
+                            }
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < KL; ++k)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const float de = av[c] - c0[IB + c + k];
+                            Sz[r][k][c] = fmaf(de, de, Sz[r][k][c]);
+                        }
+                }
+                if (out_step) {
+#pragma unroll
+                    for (int k = 0; k < KL; ++k)
+                        *reinterpret_cast<float4*>(Szb + (k * C::HY + ya) * C::PSZ + 4 * gi) =
+                            make_float4(Sz[r][k][0], Sz[r][k][1], Sz[r][k][2], Sz[r][k][3]);
+                }
+            }
+        }
+        __syncthreads();  // Sz rows written; step t's A buffer free
+        if (s_abort) break;
+        if (!out_step) continue;
+        if (tid == 0 && d + 1 < TD) issueD(lastD = d + 1);
+
+        // B: x box sums along a halo row, written over the first 32 floats of the same row
+        // (the whole row is in registers first).
+        if (okB) {
+            float* row = Szb + tid * C::PSZ;
+            constexpr int NV = (C::MA + C::HX + 3) / 4;
+            float v[4 * NV];
+#pragma unroll
+            for (int q = 0; q < NV; ++q)
+                *reinterpret_cast<float4*>(&v[4 * q]) = *reinterpret_cast<const float4*>(row + 4 * q);
+            float o[C::CX];
+            float run[2];
+#pragma unroll
+            for (int sg = 0; sg < 2; ++sg) {
+                run[sg] = 0.f;
+#pragma unroll
+                for (int x = 0; x <= 2 * N; ++x) run[sg] += v[C::MA + 16 * sg + x];
+                o[16 * sg] = run[sg];
+            }
+#pragma unroll
+            for (int j = 1; j < 16; ++j)
+#pragma unroll
+                for (int sg = 0; sg < 2; ++sg) {
+                    const int jj = 16 * sg + j;
+                    run[sg] += v[C::MA + jj + 2 * N] - v[C::MA + jj - 1];
+                    o[jj] = run[sg];
+                }
+#pragma unroll
+            for (int q = 0; q < C::CX / 4; ++q)
+                *reinterpret_cast<float4*>(row + 4 * q) =
+                    make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+        }
+        __syncthreads();
+        // C: y box sums down the output columns, in place (row y becomes D).
+        if (okC) {
+            const int k = tid >> 5, j = tid & 31;
+            float* col = Szb + k * C::HY * C::PSZ + j;
+            float u[C::HY];
+#pragma unroll
+            for (int yh = 0; yh < C::HY; ++yh) u[yh] = col[yh * C::PSZ];
+            float run[2];
+#pragma unroll
+            for (int sg = 0; sg < 2; ++sg) {
+                run[sg] = 0.f;
+#pragma unroll
+                for (int y = 0; y <= 2 * N; ++y) run[sg] += u[8 * sg + y];
+                col[8 * sg * C::PSZ] = run[sg];
+            }
+#pragma unroll
+            for (int y = 1; y < 8; ++y)
+#pragma unroll
+                for (int sg = 0; sg < 2; ++sg) {
+                    const int yy = 8 * sg + y;
+                    run[sg] += u[yy + 2 * N] - u[yy - 1];
+                    col[yy * C::PSZ] = run[sg];
+                }
+        }
+        __syncthreads();
+        // D: weights and accumulation for voxels (X0 + j, Y0 + y, z) and (.., Y0 + y + 8, z).
+        {
+            const int db = d & 1;
+            const bool okDw = mbar_wait_bounded(&barD[db], (d >> 1) & 1);
+            if (!okDw) {
+                raise_device_error(a.errword, DEVERR_TMA_TIMEOUT);
+                s_abort = 1;
+            } else if (okD) {
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int y = vy + 8 * u, j = vj;
+                    const Elem* cpl = reinterpret_cast<const Elem*>(dbuf(db)) + y * C::BWC + 4 + N +
+                                      j + C::CB + KB;
+                    float zl[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
+#pragma unroll
+                    for (int k = 0; k < KL; ++k) {
+                        const float w = ex2_neg(Szb[(k * C::HY + y) * C::PSZ + j]);
+                        zl[k & 1] += w;
+                        nl[k & 1] = fmaf(w, to_f32(cpl[k]), nl[k & 1]);
+                    }
+                    if (vin[u]) {
+                        if constexpr (C::KAHAN) {
+                            acck[vo[u]] = kahan_step(prevk[u], zl[0] + zl[1], nl[0] + nl[1]);
+                        } else {
+                            acc[vo[u]] = make_float2(prev[u].x + (zl[0] + zl[1]),
+                                                     prev[u].y + (nl[0] + nl[1]));
+                        }
+                    }
+                }
+            }
+        }
+        ++d;
+    }
+    if (tid == 0 && s_abort) {
+        mbar_wait_bounded(&barA[lastA & 1], (lastA >> 1) & 1);
+        mbar_wait_bounded(&barD[lastD & 1], (lastD >> 1) & 1);
+    }
+}
+
+template <int M, int N, typename Elem>
+__global__ void __launch_bounds__(256, 2)
+    nlm3d_lpx_kernel(const __grid_constant__ CUtensorMap mapR,
+                     const __grid_constant__ CUtensorMap mapC,
+                     const __grid_constant__ CUtensorMap mapD, const LpArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int chunk = blockIdx.z % a.nzc, part = blockIdx.z / a.nzc;  // part = 2 * split + half
+    if (part & 1)
+        lpx_body<M, N, Elem, 1>(&mapR, &mapC, &mapD, a, smem, chunk, part);
+    else
+        lpx_body<M, N, Elem, 0>(&mapR, &mapC, &mapD, a, smem, chunk, part);
+}
+
+// out = (num_0 + ... + num_{P-1}) / (Z_0 + ... + Z_{P-1}) over the voxels [v0, v0 + n) of
+// P accumulator buffers (pass halves and x-offset halves), always added in buffer order.
+// KAHAN: the buffers hold (Z, num, cZ, cnum) Kahan pairs; each contributes its sum minus
+// its compensation.
 template <bool KAHAN>
 __global__ void __launch_bounds__(256) lp_combine_kernel(const void* __restrict__ accv,
-                                                         size_t stride, size_t v0, size_t n,
-                                                         float inv_scale, float* __restrict__ out,
+                                                         size_t stride, int nparts, size_t v0,
+                                                         size_t n, float inv_scale,
+                                                         float* __restrict__ out,
                                                          float* __restrict__ zsum) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         const size_t v = v0 + i;
-        float zt, nt;
-        if constexpr (KAHAN) {
-            const float4* acc = static_cast<const float4*>(accv);
-            const float4 h0 = acc[v], h1 = acc[stride + v];
-            zt = (h0.x - h0.z) + (h1.x - h1.z);
-            nt = (h0.y - h0.w) + (h1.y - h1.w);
-        } else {
-            const float2* acc = static_cast<const float2*>(accv);
-            const float2 h0 = acc[v], h1 = acc[stride + v];
-            zt = h0.x + h1.x;
-            nt = h0.y + h1.y;
+        float zt = 0.f, nt = 0.f;
+        for (int p = 0; p < nparts; ++p) {
+            if constexpr (KAHAN) {
+                const float4 h = static_cast<const float4*>(accv)[p * stride + v];
+                zt += h.x - h.z;
+                nt += h.y - h.w;
+            } else {
+                const float2 h = static_cast<const float2*>(accv)[p * stride + v];
+                zt += h.x;
+                nt += h.y;
+            }
         }
         out[v] = nt / zt * inv_scale;
         if (zsum) zsum[v] = zt;
     }
 }
+
+// Search radii that run the two-CTAs-per-SM x-half form (nlm3d_lpx_kernel); the others
+// keep one CTA per SM with every x offset of a pass.  Measured on 512 x 512 x 16: search
+// 13 is 2-3 % faster in halves (patch 13 and 17), search 9 and 11 are 1-1.5 % slower (each
+// half loads its own reference row and a candidate window of 12 instead of 20 values for
+// 7 instead of 13 offsets, a third more stage-A loads per offset).
+template <int M>
+constexpr bool kLpXHalf = M >= 6;
 
 template <int M, int N, typename T>
 inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,
@@ -488,17 +873,16 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
                           cudaStream_t stream, int zc0, int zc1) {
     using C = Lp3d<M, N, T>;
     if (st.elem != C::ES) return cudaErrorInvalidValue;
-    CUtensorMap mapR, mapC;
+    CUtensorMap mapR, mapC, mapD;
     const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
     const uint64_t strides[2] = {(uint64_t)st.Xs * C::ES, (uint64_t)st.Xs * st.Yp * C::ES};
     const uint32_t boxR[3] = {(uint32_t)C::BWR, (uint32_t)C::HY, 1};
     const uint32_t boxC[3] = {(uint32_t)C::BWC, (uint32_t)C::HY, 1};
+    const uint32_t boxD[3] = {(uint32_t)C::BWC, (uint32_t)C::CY, 1};
     void* base = const_cast<void*>(staged);
     cudaError_t e = encode_tensor_map(&mapR, C::ES == 2, 3, dims, strides, boxR, base);
     if (e == cudaSuccess) e = encode_tensor_map(&mapC, C::ES == 2, 3, dims, strides, boxC, base);
-    if (e != cudaSuccess) return e;
-    auto kern = nlm3d_lp_kernel<M, N, T>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    if (e == cudaSuccess) e = encode_tensor_map(&mapD, C::ES == 2, 3, dims, strides, boxD, base);
     if (e != cudaSuccess) return e;
     if (zc1 < 0) zc1 = (st.Z + tz - 1) / tz;
     if (zc1 <= zc0) return cudaSuccess;
@@ -517,17 +901,35 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     a.out = out;
     a.zsum = zsum;
     a.errword = errword;
-    dim3 grid((st.X + C::CX - 1) / C::CX, (st.Y + C::CY - 1) / C::CY, (zc1 - zc0) * nsplit);
-    kern<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(mapR, mapC, a);
+    int nparts = nsplit;
+    if constexpr (kLpXHalf<M>) {
+        // two CTAs per SM, each with half of the x offsets: parts 2 * split + half
+        using X = Lpx3d<M, N, T>;
+        const uint32_t boxH[3] = {(uint32_t)X::BWH, (uint32_t)X::HY, 1};
+        e = encode_tensor_map(&mapC, X::ES == 2, 3, dims, strides, boxH, base);
+        if (e != cudaSuccess) return e;
+        auto kern = nlm3d_lpx_kernel<M, N, T>;
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, X::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        nparts = 2 * nsplit;
+        dim3 grid((st.X + X::CX - 1) / X::CX, (st.Y + X::CY - 1) / X::CY, (zc1 - zc0) * nparts);
+        kern<<<grid, X::THREADS, X::SMEM_BYTES, stream>>>(mapR, mapC, mapD, a);
+    } else {
+        auto kern = nlm3d_lp_kernel<M, N, T>;
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        dim3 grid((st.X + C::CX - 1) / C::CX, (st.Y + C::CY - 1) / C::CY, (zc1 - zc0) * nsplit);
+        kern<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(mapR, mapC, mapD, a);
+    }
     e = cudaGetLastError();
-    if (e != cudaSuccess || nsplit == 1) return e;
+    if (e != cudaSuccess || nparts == 1) return e;
     const size_t plane = (size_t)st.X * st.Y;
     const size_t v0 = (size_t)zc0 * tz * plane;
     const size_t v1 = (size_t)std::min(zc1 * tz, st.Z) * plane;
     const size_t blocks = std::min<size_t>((v1 - v0 + 255) / 256, (size_t)device_sm_count() * 8);
-    lp_combine_kernel<C::KAHAN><<<(unsigned)blocks, 256, 0, stream>>>(acc, a.part_stride, v0,
-                                                                      v1 - v0, inv_scale, out,
-                                                                      zsum);
+    lp_combine_kernel<C::KAHAN><<<(unsigned)blocks, 256, 0, stream>>>(acc, a.part_stride, nparts,
+                                                                      v0, v1 - v0, inv_scale,
+                                                                      out, zsum);
     return cudaGetLastError();
 }
 

@@ -389,7 +389,7 @@ __device__ __forceinline__ bool fwd3d_tile_pz(const CUtensorMap* map, float* til
         constexpr int JEND = C::PLANES + G - 1;
         float2 S[G][RP];
         float2 tr[G][C::K][RP];  // patch 3: squares of the last 3 planes; else differences
-        float2 mid[G][RP];       // patch 3: middle terms shared by an output plane pair
+        [[maybe_unused]] float2 mid[G][RP];  // patch 3: middle terms shared by a plane pair
         float2 cand[N + 1][OP];  // candidate centres of the last N + 1 planes, output row pairs
 #pragma unroll
         for (int j = 0; j < JEND; ++j) {

@@ -367,7 +367,8 @@ def bench_large_patch(torch, gnlm, reps=3):
             "value": round(nvox / (t * 1e-3) / 1e6, 2), "unit": "Mvoxel/s",
             "gpairs_per_s": round(pairs / (t * 1e-3) / 1e9, 1),
             "tflops": round(FLOPS_PER_PAIR * pairs / (t * 1e-3) / 1e12, 2),
-            "kernel": "nlm3d_lp_kernel<6,8>", "variant": best,
+            "kernel": "nlm3d_lpx_kernel<6,8> (x-offset halves, two CTAs per SM)",
+            "variant": best,
             "fp16_storage": {"ms": round(t16, 3), "value": round(nvox / (t16 * 1e-3) / 1e6, 2),
                              "variant": best16, "autotune_ms": [round(v, 3) for v in tune16],
                              "max_abs_err_vs_fp64": float(np.abs(d16).max()),

@@ -56,10 +56,12 @@ def test_large_patch_tiny_and_thin_volumes(torch_cuda, gnlm_lib, shape):
         assert np.abs(g16 - o).max() <= 1e-3, (shape, sr, pr)
 
 
-def test_large_patch_every_chunk_variant(torch_cuda, gnlm_lib):
-    """Each chunk depth (64, 32, 128, 16 planes) on 37 planes: partial last chunks,
-    several chunks per column."""
-    shape, sr, pr = (37, 20, 36), 2, 4
+@pytest.mark.parametrize("sr,pr", [(2, 4), (6, 3)])
+def test_large_patch_every_chunk_variant(torch_cuda, gnlm_lib, sr, pr):
+    """Each chunk depth (64, 32, 128, 16, 48, 96, 80 planes) on 37 planes: partial last
+    chunks, several chunks per column; search 13 runs the x-half form (two CTAs per
+    tile, each with half of the x offsets), whose repeated calls give the same bits."""
+    shape = (37, 20, 36)
     v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=5, sigma=0.05, seed=7, radii=(2.0, 8.0))
     o = O.nlm3d(v, sr, pr, 0.05, dtype=np.float64)
     try:
@@ -67,6 +69,7 @@ def test_large_patch_every_chunk_variant(torch_cuda, gnlm_lib):
             gnlm_lib.set_variant(3, sr, pr, var)
             g = _gpu3d(torch_cuda, gnlm_lib, v, sr, pr, 0.05)
             assert np.abs(g - o).max() <= TOL, var
+            assert np.array_equal(g, _gpu3d(torch_cuda, gnlm_lib, v, sr, pr, 0.05)), var
     finally:
         gnlm_lib.set_variant(3, sr, pr, -1)
     best, times = gnlm_lib.autotune(3, (40, 64, 64), sr, pr)
@@ -161,6 +164,7 @@ def test_large_patch_fp16_storage_variants_split_and_host_path(torch_cuda, gnlm_
     H = sr + pr
     xs = (X + 2 * H + 7) // 8 * 8
     staged = ((xs * (Y + 2 * H) * (Z + 2 * H) * 2 + 255) // 256) * 256
+    # two Kahan accumulator buffers (pass halves; search radius 6 has four)
     assert gnlm_lib.lib().nlm3d_workspace_bytes(X, Y, Z, sr, pr, gnlm_lib.NLM_FLAG_FP16_STORAGE) == \
         staged + ((2 * X * Y * Z * 16 + 255) // 256) * 256
     assert gnlm_lib.device_status() == (0, 0)
