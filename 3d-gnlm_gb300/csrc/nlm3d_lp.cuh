@@ -459,24 +459,30 @@ __global__ void __launch_bounds__(512, 1)
     }
 }
 
-// Two CTAs per SM: the x-offset halves.  With one 512-thread CTA per SM every stage
-// boundary is a barrier of the whole SM, and the stages (A: FMA and shared loads, B and
-// C: shared memory, D: ex2) cannot overlap.  This form gives each CTA half of a pass's
-// x offsets (half 0: ox = -M..0, half 1: ox = 1..M) of the same column tile and chunk,
-// in 256 threads and under half the shared memory, so two CTAs share an SM and one runs
-// its stages while the other waits at a barrier.  Stage B writes its x sums in place
+// The x-offset halves.  Each CTA takes half of a pass's x offsets (half 0: ox = -M..0,
+// half 1: ox = 1..M) of the same column tile and chunk, which halves the z sums a stage-A
+// thread keeps per halo row (two rows per thread fit) and the shared buffer that hands
+// them to stage B.  That room goes to a taller tile: 32 output rows under 48 halo rows
+// (384 threads, one CTA per SM), a third fewer halo rows per output than the one-CTA
+// kernel's 16 under 32; a 16-row tile (256 threads) fits two CTAs per SM instead, so one
+// runs its stages while the other waits at a barrier.  Stage B writes its x sums in place
 // over the Sz row it read (no separate Sx buffer), the candidate plane boxes cover only
 // the half's window, and every CTA accumulates into its own (Z, num) buffer: part
 // 2 * (pass half) + (x half), added in that order by lp_combine_kernel.
-template <int M, int N, typename T>
+template <int M, int N, typename T, int CYT = 16>
 struct Lpx3d {
     using G = Lp3d<M, N, T>;
-    static constexpr int ES = G::ES, EA = G::EA, K = G::K, CX = G::CX, CY = G::CY, H = G::H;
-    static constexpr int HX = G::HX, HY = G::HY, R = G::R, G0 = G::G0, NG = G::NG, MA = G::MA;
+    static constexpr int ES = G::ES, EA = G::EA, K = G::K, CX = G::CX, H = G::H;
+    static constexpr int HX = G::HX, R = G::R, G0 = G::G0, NG = G::NG, MA = G::MA;
     static constexpr int PSZ = G::PSZ, BWR = G::BWR, RO = G::RO, BWC = G::BWC, CB = G::CB;
     static constexpr bool KAHAN = G::KAHAN;
+    static constexpr int CY = CYT;             // output rows per tile (16 or 32)
+    static constexpr int HY = CY + 2 * N;      // halo rows
     static constexpr int KH = M + 1;           // x offsets of half 0 (half 1 has M)
-    static constexpr int THREADS = 256;
+    static constexpr int THREADS = CY == 16 ? 256 : 384;
+    static constexpr int RS = THREADS / 16;    // stage-A row slots: rows ya and ya + RS
+    static constexpr int ND = (CX * CY + THREADS - 1) / THREADS;  // stage-D voxels per thread
+    static constexpr int MINB = CY == 16 ? 2 : 1;                 // CTAs per SM
     static constexpr int WG = NG + R;          // 4-column groups of a half's candidate box
     // Half h's candidate box starts at layout group h ? G0 : G0 - R; FP16 boxes start on a
     // 16-byte (8-element) boundary, 4 elements early when that group is even.
@@ -495,19 +501,19 @@ struct Lpx3d {
     static constexpr int D_OFF = A_OFF + 2 * ABUF;
     static constexpr int BAR_OFF = D_OFF + 2 * DC_SLOT;
     static constexpr int SMEM_BYTES = BAR_OFF + 64;
-    static_assert(HY <= 32, "stage A: two halo rows per thread");
+    static_assert(HY <= 2 * RS, "stage A: two halo rows per thread");
     static_assert(KH * HY <= THREADS && KH * CX <= THREADS, "one stage B / C item per thread");
-    static_assert(CX * CY == 2 * THREADS, "two stage-D voxels per thread");
+    static_assert(THREADS % 32 == 0 && CY % 2 == 0, "stage D: whole warps, two y chains");
     static_assert(4 * WG + CB0 <= BWH && 4 * WG + CB1 <= BWH, "half box");
-    static_assert(BWH <= 256 && (BWH * ES) % 16 == 0, "TMA box");
-    static_assert(SMEM_BYTES + 1024 <= 114 * 1024, "two CTAs per SM");
+    static_assert(BWH <= 256 && (BWH * ES) % 16 == 0 && HY <= 256, "TMA box");
+    static_assert((SMEM_BYTES + 1024) * MINB <= 228 * 1024, "CTAs per SM");
 };
 
-template <int M, int N, typename Elem, int HALF>
+template <int M, int N, typename Elem, int HALF, int CYT>
 __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensorMap* mapC,
                                          const CUtensorMap* mapD, const LpArgs& a,
                                          unsigned char* smem, int chunk, int part) {
-    using C = Lpx3d<M, N, Elem>;
+    using C = Lpx3d<M, N, Elem, CYT>;
     constexpr int KL = HALF ? M : M + 1;          // x offsets of this half
     constexpr int KB = HALF ? M + 1 : 0;          // ox + M of the half's first x offset
     constexpr int OG = HALF ? C::G0 : C::G0 - C::R;  // candidate box origin (layout group)
@@ -581,18 +587,18 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
     }
 
     // Stage A: 16 lanes per halo row, lane gi < NG owns columns 4*(G0+gi) .. +3 of rows
-    // ya0 and ya0 + 16.
+    // ya0 and ya0 + RS.
     const int gi = tid & 15, ya0 = tid >> 4;
     bool hasA[2];
 #pragma unroll
-    for (int r = 0; r < 2; ++r) hasA[r] = gi < C::NG && ya0 + 16 * r < C::HY;
+    for (int r = 0; r < 2; ++r) hasA[r] = gi < C::NG && ya0 + C::RS * r < C::HY;
     bool okB = tid < KL * C::HY, okC = tid < KL * C::CX, okD = true;
     if constexpr (kBoundsCheck) {
         const long long szn = (long long)KL * C::HY * C::PSZ;
 #pragma unroll
         for (int r = 0; r < 2; ++r)
             if (hasA[r]) {
-                const int ya = ya0 + 16 * r;
+                const int ya = ya0 + C::RS * r;
                 hasA[r] = range_ok(a.errword, ya * C::BWR + 4 * gi + C::RO,
                                    ya * C::BWR + 4 * gi + C::RO + 3, C::REF_TX / C::ES) &&
                           range_ok(a.errword, ya * C::BWH + 4 * gi + CBh,
@@ -609,10 +615,10 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
             okC = range_ok(a.errword, k * C::HY * C::PSZ + j,
                            k * C::HY * C::PSZ + j + (C::HY - 1) * C::PSZ, szn);
         }
-        const int y = tid >> 5, j = tid & 31;
-        okD = range_ok(a.errword, y * C::PSZ + j, ((KL - 1) * C::HY + y + 8) * C::PSZ + j, szn) &&
+        const int y = tid >> 5, j = tid & 31, yl = min(C::CY - 1, y + (C::ND - 1) * (C::THREADS / 32));
+        okD = range_ok(a.errword, y * C::PSZ + j, ((KL - 1) * C::HY + yl) * C::PSZ + j, szn) &&
               range_ok(a.errword, y * C::BWC + 4 + N + j + C::CB + KB,
-                       (y + 8) * C::BWC + 4 + N + j + C::CB + KB + KL - 1, C::DC_TX / C::ES);
+                       yl * C::BWC + 4 + N + j + C::CB + KB + KL - 1, C::DC_TX / C::ES);
     }
     float Sz[2][KL][4];
 
@@ -629,17 +635,18 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
                     for (int c = 0; c < 4; ++c) Sz[r][k][c] = 0.f;
         }
         const bool out_step = s >= N;
-        // the two voxels' sums from earlier passes, requested early
+        // the thread's voxels' sums from earlier passes, requested early (voxel u: tile row
+        // vy + u * THREADS / 32, column vj)
         const int vy = tid >> 5, vj = tid & 31;
         const int vx = X0 + vj, vz = Z0 + (s - N);
-        size_t vo[2];
-        bool vin[2];
-        float2 prev[2];
-        float4 prevk[2];
+        size_t vo[C::ND];
+        bool vin[C::ND];
+        float2 prev[C::ND];
+        float4 prevk[C::ND];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int vyy = Y0 + vy + 8 * u;
-            vin[u] = out_step && vx < a.X && vyy < a.Y;
+        for (int u = 0; u < C::ND; ++u) {
+            const int vr = vy + u * (C::THREADS / 32), vyy = Y0 + vr;
+            vin[u] = out_step && vr < C::CY && vx < a.X && vyy < a.Y;
             vo[u] = ((size_t)vz * a.Y + vyy) * a.X + vx;
             prev[u] = make_float2(0.f, 0.f);
             prevk[u] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -660,7 +667,7 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 if (!hasA[r]) continue;
-                const int ya = ya0 + 16 * r;
+                const int ya = ya0 + C::RS * r;
                 const Elem* ref0 = reinterpret_cast<const Elem*>(abuf(b)) + C::RO;
                 const Elem* ref1 = ref0 + C::REF_SLOT / C::ES;
                 const Elem* cand0 = reinterpret_cast<const Elem*>(abuf(b) + 2 * C::REF_SLOT) + CBh;
@@ -759,25 +766,26 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
             float u[C::HY];
 #pragma unroll
             for (int yh = 0; yh < C::HY; ++yh) u[yh] = col[yh * C::PSZ];
+            constexpr int HC = C::CY / 2;  // outputs per running sum
             float run[2];
 #pragma unroll
             for (int sg = 0; sg < 2; ++sg) {
                 run[sg] = 0.f;
 #pragma unroll
-                for (int y = 0; y <= 2 * N; ++y) run[sg] += u[8 * sg + y];
-                col[8 * sg * C::PSZ] = run[sg];
+                for (int y = 0; y <= 2 * N; ++y) run[sg] += u[HC * sg + y];
+                col[HC * sg * C::PSZ] = run[sg];
             }
 #pragma unroll
-            for (int y = 1; y < 8; ++y)
+            for (int y = 1; y < HC; ++y)
 #pragma unroll
                 for (int sg = 0; sg < 2; ++sg) {
-                    const int yy = 8 * sg + y;
+                    const int yy = HC * sg + y;
                     run[sg] += u[yy + 2 * N] - u[yy - 1];
                     col[yy * C::PSZ] = run[sg];
                 }
         }
         __syncthreads();
-        // D: weights and accumulation for voxels (X0 + j, Y0 + y, z) and (.., Y0 + y + 8, z).
+        // D: weights and accumulation for the thread's voxels (X0 + j, Y0 + y, z).
         {
             const int db = d & 1;
             const bool okDw = mbar_wait_bounded(&barD[db], (d >> 1) & 1);
@@ -786,8 +794,9 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
                 s_abort = 1;
             } else if (okD) {
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const int y = vy + 8 * u, j = vj;
+                for (int u = 0; u < C::ND; ++u) {
+                    const int y = vy + u * (C::THREADS / 32), j = vj;
+                    if (y >= C::CY) continue;
                     const Elem* cpl = reinterpret_cast<const Elem*>(dbuf(db)) + y * C::BWC + 4 + N +
                                       j + C::CB + KB;
                     float zl[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
@@ -816,17 +825,17 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
     }
 }
 
-template <int M, int N, typename Elem>
-__global__ void __launch_bounds__(256, 2)
+template <int M, int N, typename Elem, int CYT>
+__global__ void __launch_bounds__(Lpx3d<M, N, Elem, CYT>::THREADS, Lpx3d<M, N, Elem, CYT>::MINB)
     nlm3d_lpx_kernel(const __grid_constant__ CUtensorMap mapR,
                      const __grid_constant__ CUtensorMap mapC,
                      const __grid_constant__ CUtensorMap mapD, const LpArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int chunk = blockIdx.z % a.nzc, part = blockIdx.z / a.nzc;  // part = 2 * split + half
     if (part & 1)
-        lpx_body<M, N, Elem, 1>(&mapR, &mapC, &mapD, a, smem, chunk, part);
+        lpx_body<M, N, Elem, 1, CYT>(&mapR, &mapC, &mapD, a, smem, chunk, part);
     else
-        lpx_body<M, N, Elem, 0>(&mapR, &mapC, &mapD, a, smem, chunk, part);
+        lpx_body<M, N, Elem, 0, CYT>(&mapR, &mapC, &mapD, a, smem, chunk, part);
 }
 
 // out = (num_0 + ... + num_{P-1}) / (Z_0 + ... + Z_{P-1}) over the voxels [v0, v0 + n) of
@@ -859,13 +868,17 @@ __global__ void __launch_bounds__(256) lp_combine_kernel(const void* __restrict_
     }
 }
 
-// Search radii that run the two-CTAs-per-SM x-half form (nlm3d_lpx_kernel); the others
-// keep one CTA per SM with every x offset of a pass.  Measured on 512 x 512 x 16: search
-// 13 is 2-3 % faster in halves (patch 13 and 17), search 9 and 11 are 1-1.5 % slower (each
-// half loads its own reference row and a candidate window of 12 instead of 20 values for
-// 7 instead of 13 offsets, a third more stage-A loads per offset).
+// Search radii that run the x-half form (nlm3d_lpx_kernel); the others keep every x
+// offset of a pass in one CTA (nlm3d_lp_kernel).  Measured on 512 x 512 x 16 with 32-row
+// x-half tiles against the one-CTA kernel: search 13 -11 %, search 11 -2 to -10 %, search 9
+// -1 to -4 %; search 7 and below +1 to +12 % (with few x offsets, halving them halves the
+// candidate windows' reuse).
 template <int M>
-constexpr bool kLpXHalf = M >= 6;
+constexpr bool kLpXHalf = M >= 4;
+// Output rows per x-half tile: 32 (one CTA of 384 threads per SM, 48 halo rows for 32 output
+// rows) rather than 16 (two CTAs of 256 threads per SM, 32 halo rows for 16): at search 13,
+// patch 17 the taller tile is 11 % faster (512 x 512 x 128: 207 -> 183 ms).
+constexpr int kLpXHalfRows = 32;
 
 template <int M, int N, typename T>
 inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,
@@ -903,12 +916,16 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     a.errword = errword;
     int nparts = nsplit;
     if constexpr (kLpXHalf<M>) {
-        // two CTAs per SM, each with half of the x offsets: parts 2 * split + half
-        using X = Lpx3d<M, N, T>;
+        // CTAs with half of the x offsets each: parts 2 * split + half
+        using X = Lpx3d<M, N, T, kLpXHalfRows>;
+        const uint32_t boxRx[3] = {(uint32_t)X::BWR, (uint32_t)X::HY, 1};
         const uint32_t boxH[3] = {(uint32_t)X::BWH, (uint32_t)X::HY, 1};
-        e = encode_tensor_map(&mapC, X::ES == 2, 3, dims, strides, boxH, base);
+        const uint32_t boxDx[3] = {(uint32_t)X::BWC, (uint32_t)X::CY, 1};
+        e = encode_tensor_map(&mapR, X::ES == 2, 3, dims, strides, boxRx, base);
+        if (e == cudaSuccess) e = encode_tensor_map(&mapC, X::ES == 2, 3, dims, strides, boxH, base);
+        if (e == cudaSuccess) e = encode_tensor_map(&mapD, X::ES == 2, 3, dims, strides, boxDx, base);
         if (e != cudaSuccess) return e;
-        auto kern = nlm3d_lpx_kernel<M, N, T>;
+        auto kern = nlm3d_lpx_kernel<M, N, T, kLpXHalfRows>;
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, X::SMEM_BYTES);
         if (e != cudaSuccess) return e;
         nparts = 2 * nsplit;
