@@ -192,12 +192,12 @@ bool nlm3d_fwd_large_patch(int sr, int pr, bool fp16) {
 }
 
 // Up to four accumulator buffers: the large-patch launcher may split each tile's passes
-// into two halves (nlm3d_lp_split) and, from search radius 4, each pass's x offsets into
+// into two halves (nlm3d_lp_split) and, from search radius 3, each pass's x offsets into
 // two halves run by separate CTAs (kLpXHalf).  (Z, num) float2 per voxel, or with FP16
 // storage the Kahan pairs (Z, num, cZ, cnum) float4.
 size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16) {
     if (!nlm3d_fwd_large_patch(sr, pr, fp16)) return 0;
-    const size_t parts = sr >= 4 ? 4 : 2;
+    const size_t parts = sr >= 3 ? 4 : 2;
     return align_up(parts * X * Y * Z * (fp16 ? sizeof(float4) : sizeof(float2)), kAlign);
 }
 

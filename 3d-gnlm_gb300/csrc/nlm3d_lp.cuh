@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(512, 1)
 // The x-offset halves.  Each CTA takes half of a pass's x offsets (half 0: ox = -M..0,
 // half 1: ox = 1..M) of the same column tile and chunk, which halves the z sums a stage-A
 // thread keeps per halo row (two rows per thread fit) and the shared buffer that hands
-// them to stage B.  That room goes to a taller tile: 32 output rows under 48 halo rows
-// (384 threads, one CTA per SM), a third fewer halo rows per output than the one-CTA
+// them to stage B.  That room goes to a taller tile: 48 output rows under 64 halo rows
+// (512 threads, one CTA per SM) or 32 under 48 (384 threads), against the one-CTA
 // kernel's 16 under 32; a 16-row tile (256 threads) fits two CTAs per SM instead, so one
 // runs its stages while the other waits at a barrier.  Stage B writes its x sums in place
 // over the Sz row it read (no separate Sx buffer), the candidate plane boxes cover only
@@ -479,7 +479,7 @@ struct Lpx3d {
     static constexpr int CY = CYT;             // output rows per tile (16 or 32)
     static constexpr int HY = CY + 2 * N;      // halo rows
     static constexpr int KH = M + 1;           // x offsets of half 0 (half 1 has M)
-    static constexpr int THREADS = CY == 16 ? 256 : 384;
+    static constexpr int THREADS = CY == 16 ? 256 : (CY == 32 ? 384 : 512);
     static constexpr int RS = THREADS / 16;    // stage-A row slots: rows ya and ya + RS
     static constexpr int ND = (CX * CY + THREADS - 1) / THREADS;  // stage-D voxels per thread
     static constexpr int MINB = CY == 16 ? 2 : 1;                 // CTAs per SM
@@ -498,8 +498,9 @@ struct Lpx3d {
     static constexpr int ABUF = 2 * REF_SLOT + 2 * CAND_SLOT;
     static constexpr int SZ_OFF = 0;
     static constexpr int A_OFF = cround(KH * HY * PSZ * 4, 128);
+    static constexpr int NDB = CY >= 48 ? 1 : 2;  // stage-D candidate buffers
     static constexpr int D_OFF = A_OFF + 2 * ABUF;
-    static constexpr int BAR_OFF = D_OFF + 2 * DC_SLOT;
+    static constexpr int BAR_OFF = D_OFF + NDB * DC_SLOT;
     static constexpr int SMEM_BYTES = BAR_OFF + 64;
     static_assert(HY <= 2 * RS, "stage A: two halo rows per thread");
     static_assert(KH * HY <= THREADS && KH * CX <= THREADS, "one stage B / C item per thread");
@@ -539,7 +540,7 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
     const int TD = P * TZc;
 
     auto abuf = [&](int b) { return smem + C::A_OFF + b * C::ABUF; };
-    auto dbuf = [&](int b) { return smem + C::D_OFF + b * C::DC_SLOT; };
+    auto dbuf = [&](int b) { return smem + C::D_OFF + (C::NDB == 1 ? 0 : b) * C::DC_SLOT; };
     // Thread 0: loads of step t's planes (as in nlm3d_lp_kernel; candidates: the half's box).
     auto issueA = [&](int t) {
         const int b = t & 1, lp = t / SPP, s = t - lp * SPP, pass = pb + lp;
@@ -567,7 +568,7 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
     };
     // Thread 0: stage D's candidate plane of output step d (CY rows, full x window).
     auto issueD = [&](int d) {
-        const int b = d & 1, lp = d / TZc, q = d - lp * TZc, pass = pb + lp;
+        const int b = C::NDB == 1 ? 0 : d & 1, lp = d / TZc, q = d - lp * TZc, pass = pb + lp;
         const int oz = pass / C::K - M, oy = pass % C::K - M;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&barD[b], C::DC_TX);
@@ -725,7 +726,11 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
         __syncthreads();  // Sz rows written; step t's A buffer free
         if (s_abort) break;
         if (!out_step) continue;
-        if (tid == 0 && d + 1 < TD) issueD(lastD = d + 1);
+        if constexpr (C::NDB == 2) {
+            if (tid == 0 && d + 1 < TD) issueD(lastD = d + 1);
+        } else {  // one buffer: step d's box, once stage D of step d - 1 is done (barrier above)
+            if (tid == 0 && d >= 1) issueD(lastD = d);
+        }
 
         // B: x box sums along a halo row, written over the first 32 floats of the same row
         // (the whole row is in registers first).
@@ -787,8 +792,8 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
         __syncthreads();
         // D: weights and accumulation for the thread's voxels (X0 + j, Y0 + y, z).
         {
-            const int db = d & 1;
-            const bool okDw = mbar_wait_bounded(&barD[db], (d >> 1) & 1);
+            const int db = C::NDB == 1 ? 0 : d & 1;
+            const bool okDw = mbar_wait_bounded(&barD[db], C::NDB == 1 ? d & 1 : (d >> 1) & 1);
             if (!okDw) {
                 raise_device_error(a.errword, DEVERR_TMA_TIMEOUT);
                 s_abort = 1;
@@ -821,7 +826,10 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
     }
     if (tid == 0 && s_abort) {
         mbar_wait_bounded(&barA[lastA & 1], (lastA >> 1) & 1);
-        mbar_wait_bounded(&barD[lastD & 1], (lastD >> 1) & 1);
+        if constexpr (C::NDB == 1)
+            mbar_wait_bounded(&barD[0], lastD & 1);
+        else
+            mbar_wait_bounded(&barD[lastD & 1], (lastD >> 1) & 1);
     }
 }
 
@@ -869,16 +877,18 @@ __global__ void __launch_bounds__(256) lp_combine_kernel(const void* __restrict_
 }
 
 // Search radii that run the x-half form (nlm3d_lpx_kernel); the others keep every x
-// offset of a pass in one CTA (nlm3d_lp_kernel).  Measured on 512 x 512 x 16 with 32-row
-// x-half tiles against the one-CTA kernel: search 13 -11 %, search 11 -2 to -10 %, search 9
-// -1 to -4 %; search 7 and below +1 to +12 % (with few x offsets, halving them halves the
-// candidate windows' reuse).
+// offset of a pass in one CTA (nlm3d_lp_kernel).  Measured on 512 x 512 x 16 with 48-row
+// x-half tiles against the one-CTA kernel: search 13 -10 to -22 %, search 11 -1 to -16 %,
+// search 9 -4 to -14 %, search 7 -1 to -9 %; search 5 and 3 +1 to +2 % (with few x offsets,
+// halving them halves the candidate windows' reuse).
 template <int M>
-constexpr bool kLpXHalf = M >= 4;
-// Output rows per x-half tile: 32 (one CTA of 384 threads per SM, 48 halo rows for 32 output
-// rows) rather than 16 (two CTAs of 256 threads per SM, 32 halo rows for 16): at search 13,
-// patch 17 the taller tile is 11 % faster (512 x 512 x 128: 207 -> 183 ms).
-constexpr int kLpXHalfRows = 32;
+constexpr bool kLpXHalf = M >= 3;
+// Output rows per x-half tile: 48 (one CTA of 512 threads per SM, 64 halo rows for 48 output
+// rows, one stage-D candidate buffer so that the plane boxes fit), the tallest tile whose
+// FP32 buffers fit the shared memory.  At search 13, patch 17 on 512 x 512 x 128: 16-row
+// tiles (two CTAs of 256 threads per SM) 207 ms, 32-row tiles (384 threads) 183 ms, 48-row
+// tiles 167 ms.
+constexpr int kLpXHalfRows = 48;
 
 template <int M, int N, typename T>
 inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,

@@ -367,7 +367,7 @@ def bench_large_patch(torch, gnlm, reps=3):
             "value": round(nvox / (t * 1e-3) / 1e6, 2), "unit": "Mvoxel/s",
             "gpairs_per_s": round(pairs / (t * 1e-3) / 1e9, 1),
             "tflops": round(FLOPS_PER_PAIR * pairs / (t * 1e-3) / 1e12, 2),
-            "kernel": "nlm3d_lpx_kernel<6,8,float,32> (x-offset halves, 32-row tiles)",
+            "kernel": "nlm3d_lpx_kernel<6,8,float,48> (x-offset halves, 48-row tiles)",
             "variant": best,
             "fp16_storage": {"ms": round(t16, 3), "value": round(nvox / (t16 * 1e-3) / 1e6, 2),
                              "variant": best16, "autotune_ms": [round(v, 3) for v in tune16],

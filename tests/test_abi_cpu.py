@@ -83,12 +83,12 @@ def test_workspace_query_is_pure_host(L):
     assert L.nlm2d_workspace_bytes(2048, 2048, 5, 2, 0) == ((2064 * 2062 * 4 + 255) // 256) * 256
     # large patch (search 13, patch 17 on 512 x 512 x 16): staged volume padded by 14
     # (x stride rounded to 4 floats), then four buffers of one (Z, num) float pair per
-    # voxel (each tile's passes may be split between two CTAs, and from search radius 4
-    # each pass's x offsets are split between two more); search radius 3 keeps two
+    # voxel (each tile's passes may be split between two CTAs, and from search radius 3
+    # each pass's x offsets are split between two more); search radius 2 keeps two
     staged = ((540 * 540 * 44 * 4 + 255) // 256) * 256
     assert L.nlm3d_workspace_bytes(512, 512, 16, 6, 8, 0) == staged + 4 * 512 * 512 * 16 * 8
-    staged3 = ((536 * 534 * 38 * 4 + 255) // 256) * 256  # padded by 11, x stride 536
-    assert L.nlm3d_workspace_bytes(512, 512, 16, 3, 8, 0) == staged3 + 2 * 512 * 512 * 16 * 8
+    staged2 = ((532 * 532 * 36 * 4 + 255) // 256) * 256  # padded by 10, x stride 532
+    assert L.nlm3d_workspace_bytes(512, 512, 16, 2, 8, 0) == staged2 + 2 * 512 * 512 * 16 * 8
 
 
 @pytest.mark.parametrize("args,code", [

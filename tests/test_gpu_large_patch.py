@@ -60,7 +60,8 @@ def test_large_patch_tiny_and_thin_volumes(torch_cuda, gnlm_lib, shape):
 def test_large_patch_every_chunk_variant(torch_cuda, gnlm_lib, sr, pr):
     """Each chunk depth (64, 32, 128, 16, 48, 96, 80 planes) on 37 planes: partial last
     chunks, several chunks per column; search 9 and 13 run the x-half form (two CTAs per
-    tile, each with half of the x offsets), whose repeated calls give the same bits."""
+    tile, each with half of the x offsets, 48-row tiles), whose repeated calls give the
+    same bits."""
     shape = (37, 20, 36)
     v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=5, sigma=0.05, seed=7, radii=(2.0, 8.0))
     o = O.nlm3d(v, sr, pr, 0.05, dtype=np.float64)
@@ -164,7 +165,7 @@ def test_large_patch_fp16_storage_variants_split_and_host_path(torch_cuda, gnlm_
     H = sr + pr
     xs = (X + 2 * H + 7) // 8 * 8
     staged = ((xs * (Y + 2 * H) * (Z + 2 * H) * 2 + 255) // 256) * 256
-    # four Kahan accumulator buffers from search radius 4 (pass halves x x-offset halves)
+    # four Kahan accumulator buffers from search radius 3 (pass halves x x-offset halves)
     assert gnlm_lib.lib().nlm3d_workspace_bytes(X, Y, Z, sr, pr, gnlm_lib.NLM_FLAG_FP16_STORAGE) == \
         staged + ((4 * X * Y * Z * 16 + 255) // 256) * 256
     assert gnlm_lib.device_status() == (0, 0)
