@@ -12,17 +12,20 @@ int device_sm_count() {
     return sms;
 }
 
-// Pass split of a whole volume (one CTA per SM): two half-pass CTAs per tile when
-// that fills the last wave better, estimated as ceil(2n / SMs) / 2 against
-// ceil(n / SMs) waves of full-pass CTAs.  Depends only on the volume, the chunk
-// depth and the device, so every launch over one volume (whole or by chunk
-// ranges) makes the same choice and the sums are the same bits.
-int nlm3d_lp_split(int X, int Y, int Z, int tz) {
+// Pass split of a whole volume: two half-pass CTAs per tile (per x part) when that fills
+// the last wave better, estimated as ceil(2n / slots) / 2 against ceil(n / slots) waves
+// for n = tiles x chunks x x-parts full-pass CTAs and slots = SMs x CTAs per SM.
+// Depends only on the volume, the chunk depth, the tile geometry and the device, so
+// every launch over one volume (whole or by chunk ranges) makes the same choice and the
+// sums are the same bits.
+int nlm3d_lp_split(int X, int Y, int Z, int tz, int tile_x, int tile_y, int xparts,
+                   int ctas_per_sm) {
     if (tz <= 0) return 1;
-    const long long n = (long long)((X + 31) / 32) * ((Y + 15) / 16) * ((Z + tz - 1) / tz);
-    const long long sms = device_sm_count();
-    const double one = (double)((n + sms - 1) / sms);
-    const double two = (double)((2 * n + sms - 1) / sms) / 2.0;
+    const long long n = (long long)((X + tile_x - 1) / tile_x) * ((Y + tile_y - 1) / tile_y) *
+                        ((Z + tz - 1) / tz) * xparts;
+    const long long slots = (long long)device_sm_count() * ctas_per_sm;
+    const double one = (double)((n + slots - 1) / slots);
+    const double two = (double)((2 * n + slots - 1) / slots) / 2.0;
     return two < 0.97 * one ? 2 : 1;
 }
 

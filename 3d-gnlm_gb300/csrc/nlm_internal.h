@@ -74,7 +74,8 @@ size_t nlm3d_fwd_extra_bytes(int X, int Y, int Z, int sr, int pr, bool fp16);
 // per-voxel (Z, num) float2, or (Z, num, cZ, cnum) float4 Kahan pairs for FP16.
 int nlm3d_lp_tile_z(int variant);
 bool nlm3d_lp_supported(int sr, int pr);
-int nlm3d_lp_split(int X, int Y, int Z, int tz);
+int nlm3d_lp_split(int X, int Y, int Z, int tz, int tile_x, int tile_y, int xparts,
+                   int ctas_per_sm);
 cudaError_t launch_nlm3d_lp(const Staging& st, const void* staged, int sr, int pr, bool fp16,
                             int variant, float inv_scale, float* out, float* zsum, void* acc,
                             unsigned int* errword, cudaStream_t stream, int zc0, int zc1);

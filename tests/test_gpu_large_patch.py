@@ -148,7 +148,7 @@ def test_large_patch_fp16_storage_variants_split_and_host_path(torch_cuda, gnlm_
             assert np.abs(g - o).max() <= TOL_F16, var
     finally:
         gnlm_lib.set_variant(3, sr, pr, -1, fp16_storage=True)
-    for shp in [(4, 300, 250), (4, 144, 250)]:
+    for shp in [(4, 912, 250), (4, 432, 250)]:  # one whole wave, a split grid (see below)
         w, _ = phantom.ellipsoid_phantom(shp, n_ellipsoids=8, sigma=0.05, seed=shp[1],
                                          radii=(3.0, 20.0))
         g = _gpu3d(torch, gnlm_lib, w, 1, 3, 0.05, fp16_storage=True)
@@ -202,10 +202,12 @@ def test_large_patch_sweep_size_fp16_storage(torch_cuda, gnlm_lib):
 def test_large_patch_split_and_whole_passes(torch_cuda, gnlm_lib):
     """One CTA per SM: a grid that leaves the last wave mostly idle splits each tile's
     passes into two halves with separate accumulators, added by a combine kernel;
-    a grid of whole waves does not.  On a 152-SM GB300, 250 x 300 x 4 is 8 x 19 tiles
-    = exactly one wave (no split) and 250 x 144 x 4 is 8 x 9 tiles, under half a wave
-    (split).  Both match the FP64 oracle, and repeated calls give the same bits."""
-    for shape in [(4, 300, 250), (4, 144, 250)]:
+    a grid of whole waves does not (and the combine kernel still writes num / Z from the
+    one buffer).  On a 152-SM GB300 with 32 x 48 tiles and every x offset per CTA (search
+    3), 250 x 912 x 4 is 8 x 19 tiles = exactly one wave (no split) and 250 x 432 x 4 is
+    8 x 9 tiles, under half a wave (split).  Both match the FP64 oracle, and repeated calls
+    give the same bits."""
+    for shape in [(4, 912, 250), (4, 432, 250)]:
         v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=8, sigma=0.05, seed=shape[1],
                                          radii=(3.0, 20.0))
         g = _gpu3d(torch_cuda, gnlm_lib, v, 1, 3, 0.05)
