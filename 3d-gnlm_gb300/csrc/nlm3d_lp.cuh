@@ -138,11 +138,12 @@ struct Lpx3d {
     static constexpr int MINB = CY == 16 ? 2 : 1;                 // CTAs per SM
     static constexpr int WN = XS == 2 ? R + 1 : 2 * R + 1;  // candidate float4s per row
     static constexpr int WG = NG + WN - 1;     // 4-column groups of a candidate box
-    // Half h's candidate box starts at layout group h ? G0 : G0 - R; FP16 boxes start on a
-    // 16-byte (8-element) boundary, 4 elements early when that group is even.
+    // The candidate box starts at layout group G0 - R (half 0, or every x offset) or G0
+    // (half 1); FP16 boxes start on a 16-byte (8-element) boundary, 4 elements early when
+    // that group is even.
     static constexpr int CB0 = ES == 2 && (G0 - R) % 2 == 0 ? 4 : 0;
     static constexpr int CB1 = ES == 2 && G0 % 2 == 0 ? 4 : 0;
-    static constexpr int BWH = cround(4 * WG + (ES == 2 ? 4 : 0), EA);  // half box width
+    static constexpr int BWH = cround(4 * WG + (ES == 2 ? 4 : 0), EA);  // candidate box width
     static constexpr int REF_TX = BWR * HY * ES;
     static constexpr int CAND_TX = BWH * HY * ES;
     static constexpr int REF_SLOT = cround(REF_TX, 128);
