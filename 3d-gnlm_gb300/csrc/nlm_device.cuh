@@ -23,8 +23,9 @@ enum : unsigned int {
 // (the test library libgnlm_checked.so) read: with FAULT_SKIP_TILE_COPY set, the CTA of
 // tile (0, 0, 0) of each 3D/2D forward or adjoint launch arms its barrier for the tile
 // copy but never issues the copy, so its bounded wait runs out exactly as it would for
-// a copy that never lands.  Nothing is in flight when that CTA gives up, and its wait
-// limit is kInjectedWaitPolls so the test does not spend the full limit.
+// a copy that never lands (the large-patch kernel: the CTA at grid origin, for the planes
+// of its first step).  Nothing is in flight for that barrier when the CTA gives up, and
+// its wait limit is kInjectedWaitPolls so the test does not spend the full limit.
 enum : unsigned int { FAULT_SKIP_TILE_COPY = 0x1u };
 
 // Builds compiled with -DNLM_BOUNDS_CHECK verify, once per tile or work item, that

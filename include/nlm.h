@@ -83,7 +83,8 @@ int nlm_device_status(unsigned int* flags);
 
 /* Test hook (no counterpart in the reference): in the bounds-checked test build,
  * libgnlm_checked.so, bits = 0x1 makes the first tile (0, 0, 0) of every later 3D/2D
- * forward and adjoint launch on the current device skip its tile copy, so its bounded
+ * forward (large-patch included) and adjoint launch on the current device skip its tile
+ * copy (the large-patch kernel: the planes of its first step), so its bounded
  * wait runs out and the kernel reports 0x1 in the device error word instead of
  * hanging; that tile's outputs are left unwritten.  bits = 0 turns it off.  The
  * production library (libgnlm.so) returns NLM_ERR_UNSUPPORTED and changes nothing. */

@@ -45,6 +45,7 @@ def main():
         "2d": lambda: gnlm.nlm2d_forward(x2, 5, 2, 0.08),
         "batched": lambda: gnlm.nlm3d_forward_batched([(x, 3, 1, 0.05), (x, 2, 1, 0.06)]),
         "adjoint": lambda: gnlm.nlm3d_adjoint(x, out0, zs0, g, 3, 1, 0.05),
+        "large_patch": lambda: gnlm.nlm3d_forward(x, 4, 3, 0.05),
     }
     res = {"lib": gnlm.LIB_PATH, "cases": {}}
     for name, call in cases.items():

@@ -84,7 +84,8 @@ def test_bounded_tile_copy_waits_run_out_and_report(torch_cuda, gnlm_lib):
     assert proc.returncode == 0, proc.stderr[-2000:]
     res = json.loads(proc.stdout.strip().splitlines()[-1])
     assert res["lib"].endswith("libgnlm_checked.so")
-    assert set(res["cases"]) == {"3d_fp32", "3d_fp16_storage", "2d", "batched", "adjoint"}
+    assert set(res["cases"]) == {"3d_fp32", "3d_fp16_storage", "2d", "batched", "adjoint",
+                                 "large_patch"}
     for name, r in res["cases"].items():
         assert r["set"] == 0 and r["unset"] == 0, (name, r)
         assert r["status"] == gnlm_lib.NLM_ERR_DEVICE and r["flags"] == 0x1, (name, r)
