@@ -132,8 +132,9 @@ struct Lpx3d {
     // XS = 2: x-offset halves (KH = M + 1 offsets for half 0, M for half 1); XS = 1: every
     // x offset in one CTA (the same tall-tile layout for small search radii)
     static constexpr int KH = XS == 2 ? M + 1 : 2 * M + 1;
-    static constexpr int THREADS = CY == 16 ? 256 : (CY == 32 ? 384 : 512);
-    static constexpr int RS = THREADS / 16;    // stage-A row slots: rows ya and ya + RS
+    static constexpr int THREADS = CY == 16 ? 256 : (CY == 32 ? 384 : (CY == 48 ? 512 : 448));
+    static constexpr int RS = THREADS / 16;    // stage-A row slots: rows ya + r * RS
+    static constexpr int RA = (HY + RS - 1) / RS;  // halo rows per stage-A thread
     static constexpr int ND = (CX * CY + THREADS - 1) / THREADS;  // stage-D voxels per thread
     static constexpr int MINB = CY == 16 ? 2 : 1;                 // CTAs per SM
     static constexpr int WN = XS == 2 ? R + 1 : 2 * R + 1;  // candidate float4s per row
@@ -154,11 +155,12 @@ struct Lpx3d {
     static constexpr int SZ_OFF = 0;
     static constexpr int A_OFF = cround(KH * HY * PSZ * 4, 128);
     static constexpr int NDB = CY >= 48 ? 1 : 2;  // stage-D candidate buffers
+    static constexpr int NB = KH * HY;         // stage-B items (offset, halo row)
     static constexpr int D_OFF = A_OFF + 2 * ABUF;
     static constexpr int BAR_OFF = D_OFF + NDB * DC_SLOT;
     static constexpr int SMEM_BYTES = BAR_OFF + 64;
-    static_assert(HY <= 2 * RS, "stage A: two halo rows per thread");
-    static_assert(KH * HY <= THREADS && KH * CX <= THREADS, "one stage B / C item per thread");
+    static_assert(RA <= 3, "stage A: at most three halo rows per thread");
+    static_assert(KH * CX <= THREADS, "one stage C item per thread");
     static_assert(THREADS % 32 == 0 && CY % 2 == 0, "stage D: whole warps, two y chains");
     static_assert(4 * WG + CB0 <= BWH && 4 * WG + CB1 <= BWH, "candidate box");
     static_assert(BWH <= 256 && (BWH * ES) % 16 == 0 && HY <= 256, "TMA box");
@@ -252,14 +254,14 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
     // Stage A: 16 lanes per halo row, lane gi < NG owns columns 4*(G0+gi) .. +3 of rows
     // ya0 and ya0 + RS.
     const int gi = tid & 15, ya0 = tid >> 4;
-    bool hasA[2];
+    bool hasA[C::RA];
 #pragma unroll
-    for (int r = 0; r < 2; ++r) hasA[r] = gi < C::NG && ya0 + C::RS * r < C::HY;
-    bool okB = tid < KL * C::HY, okC = tid < KL * C::CX, okD = true;
+    for (int r = 0; r < C::RA; ++r) hasA[r] = gi < C::NG && ya0 + C::RS * r < C::HY;
+    bool okB = true, okC = tid < KL * C::CX, okD = true;
     if constexpr (kBoundsCheck) {
         const long long szn = (long long)KL * C::HY * C::PSZ;
 #pragma unroll
-        for (int r = 0; r < 2; ++r)
+        for (int r = 0; r < C::RA; ++r)
             if (hasA[r]) {
                 const int ya = ya0 + C::RS * r;
                 hasA[r] = range_ok(a.errword, ya * C::BWR + 4 * gi + C::RO,
@@ -269,9 +271,11 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
                           range_ok(a.errword, ya * C::PSZ + 4 * gi,
                                    ((KL - 1) * C::HY + ya) * C::PSZ + 4 * gi + 3, szn);
             }
-        if (okB) {
+        {  // stage-B rows: items tid, tid + THREADS, ... < KL * HY
             constexpr int NV = (C::MA + C::HX + 3) / 4;
-            okB = range_ok(a.errword, tid * C::PSZ, tid * C::PSZ + 4 * NV - 1, szn);
+            const int last = tid + ((KL * C::HY - 1 - tid) / C::THREADS) * C::THREADS;
+            if (tid < KL * C::HY)
+                okB = range_ok(a.errword, tid * C::PSZ, last * C::PSZ + 4 * NV - 1, szn);
         }
         if (okC) {
             const int k = tid >> 5, j = tid & 31;
@@ -283,7 +287,7 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
               range_ok(a.errword, y * C::BWC + 4 + N + j + C::CB + KB,
                        yl * C::BWC + 4 + N + j + C::CB + KB + KL - 1, C::DC_TX / C::ES);
     }
-    float Sz[2][KL][4];
+    float Sz[C::RA][KL][4];
 
     int d = 0;
     for (int t = 0; t < T; ++t) {
@@ -291,7 +295,7 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
         if (tid == 0 && t + 1 < T) issueA(lastA = t + 1);
         if (s == 0) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r)
+            for (int r = 0; r < C::RA; ++r)
 #pragma unroll
                 for (int k = 0; k < KL; ++k)
 #pragma unroll
@@ -329,7 +333,7 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
         }
         if (okA) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
+            for (int r = 0; r < C::RA; ++r) {
                 if (!hasA[r]) continue;
                 const int ya = ya0 + C::RS * r;
                 const Elem* ref0 = reinterpret_cast<const Elem*>(abuf(b)) + C::RO;
@@ -397,8 +401,8 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
 
         // B: x box sums along a halo row, written over the first 32 floats of the same row
         // (the whole row is in registers first).
-        if (okB) {
-            float* row = Szb + tid * C::PSZ;
+        for (int bi = tid; okB && bi < KL * C::HY; bi += C::THREADS) {
+            float* row = Szb + bi * C::PSZ;
             constexpr int NV = (C::MA + C::HX + 3) / 4;
             float v[4 * NV];
 #pragma unroll
@@ -431,26 +435,47 @@ __device__ __forceinline__ void lpx_body(const CUtensorMap* mapR, const CUtensor
         if (okC) {
             const int k = tid >> 5, j = tid & 31;
             float* col = Szb + k * C::HY * C::PSZ + j;
-            float u[C::HY];
-#pragma unroll
-            for (int yh = 0; yh < C::HY; ++yh) u[yh] = col[yh * C::PSZ];
             constexpr int HC = C::CY / 2;  // outputs per running sum
-            float run[2];
+            if constexpr (C::HY <= 64) {
+                // the whole column in registers, two interleaved running sums
+                float u[C::HY];
 #pragma unroll
-            for (int sg = 0; sg < 2; ++sg) {
-                run[sg] = 0.f;
-#pragma unroll
-                for (int y = 0; y <= 2 * N; ++y) run[sg] += u[HC * sg + y];
-                col[HC * sg * C::PSZ] = run[sg];
-            }
-#pragma unroll
-            for (int y = 1; y < HC; ++y)
+                for (int yh = 0; yh < C::HY; ++yh) u[yh] = col[yh * C::PSZ];
+                float run[2];
 #pragma unroll
                 for (int sg = 0; sg < 2; ++sg) {
-                    const int yy = HC * sg + y;
-                    run[sg] += u[yy + 2 * N] - u[yy - 1];
-                    col[yy * C::PSZ] = run[sg];
+                    run[sg] = 0.f;
+#pragma unroll
+                    for (int y = 0; y <= 2 * N; ++y) run[sg] += u[HC * sg + y];
+                    col[HC * sg * C::PSZ] = run[sg];
                 }
+#pragma unroll
+                for (int y = 1; y < HC; ++y)
+#pragma unroll
+                    for (int sg = 0; sg < 2; ++sg) {
+                        const int yy = HC * sg + y;
+                        run[sg] += u[yy + 2 * N] - u[yy - 1];
+                        col[yy * C::PSZ] = run[sg];
+                    }
+            } else {
+                // one half column at a time (fewer registers beside the z sums); the second
+                // half's rows are read before the first's writes could reach them
+#pragma unroll
+                for (int sg = 0; sg < 2; ++sg) {
+                    float u[HC + 2 * N];
+#pragma unroll
+                    for (int yh = 0; yh < HC + 2 * N; ++yh) u[yh] = col[(HC * sg + yh) * C::PSZ];
+                    float run = 0.f;
+#pragma unroll
+                    for (int y = 0; y <= 2 * N; ++y) run += u[y];
+                    col[HC * sg * C::PSZ] = run;
+#pragma unroll
+                    for (int y = 1; y < HC; ++y) {
+                        run += u[y + 2 * N] - u[y - 1];
+                        col[(HC * sg + y) * C::PSZ] = run;
+                    }
+                }
+            }
         }
         __syncthreads();
         // D: weights and accumulation for the thread's voxels (X0 + j, Y0 + y, z).
@@ -556,7 +581,12 @@ constexpr bool kLpXHalf = M >= 3;
 // tiles (two CTAs of 256 threads per SM) 207 ms, 32-row tiles (384 threads) 183 ms, 48-row
 // tiles 167 ms.  Search 3 and 5 with every x offset per CTA: 48-row against 16-row tiles
 // -18 to -28 %.
-constexpr int kLpRows = 48;
+// With FP16 plane boxes and every x offset per CTA (search 3 and 5) the buffers also fit
+// 64 output rows under 80 halo rows (448 threads, three halo rows per stage-A thread):
+// 11-16 % faster than 48 rows there, and faster than FP32.  The x-half FP16 CTAs keep 48
+// rows (64 measured 22 % slower: the seven z sums of three rows crowd the registers).
+template <typename T, int XS>
+constexpr int kLpRows = sizeof(T) == 2 && XS == 1 ? 64 : 48;
 
 template <int M, int N, typename T>
 inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,
@@ -564,7 +594,7 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
                           cudaStream_t stream, int zc0, int zc1) {
     // x-offset halves (parts 2 * split + half) or every x offset (parts = splits) per CTA
     constexpr int XS = kLpXHalf<M> ? 2 : 1;
-    using X = Lpx3d<M, N, T, kLpRows, XS>;
+    using X = Lpx3d<M, N, T, kLpRows<T, XS>, XS>;
     if (st.elem != X::ES) return cudaErrorInvalidValue;
     CUtensorMap mapR, mapC, mapD;
     const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
@@ -577,7 +607,7 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     if (e == cudaSuccess) e = encode_tensor_map(&mapC, X::ES == 2, 3, dims, strides, boxC, base);
     if (e == cudaSuccess) e = encode_tensor_map(&mapD, X::ES == 2, 3, dims, strides, boxD, base);
     if (e != cudaSuccess) return e;
-    auto kern = nlm3d_lpx_kernel<M, N, T, kLpRows, XS>;
+    auto kern = nlm3d_lpx_kernel<M, N, T, kLpRows<T, XS>, XS>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, X::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     if (zc1 < 0) zc1 = (st.Z + tz - 1) / tz;
