@@ -581,12 +581,13 @@ constexpr bool kLpXHalf = M >= 3;
 // tiles (two CTAs of 256 threads per SM) 207 ms, 32-row tiles (384 threads) 183 ms, 48-row
 // tiles 167 ms.  Search 3 and 5 with every x offset per CTA: 48-row against 16-row tiles
 // -18 to -28 %.
-// With FP16 plane boxes and every x offset per CTA (search 3 and 5) the buffers also fit
-// 64 output rows under 80 halo rows (448 threads, three halo rows per stage-A thread):
-// 11-16 % faster than 48 rows there, and faster than FP32.  The x-half FP16 CTAs keep 48
-// rows (64 measured 22 % slower: the seven z sums of three rows crowd the registers).
-template <typename T, int XS>
-constexpr int kLpRows = sizeof(T) == 2 && XS == 1 ? 64 : 48;
+// With every x offset per CTA and FP16 plane boxes (search 3 and 5), or FP32 ones at search
+// 3 (three z sums per row), the buffers also fit 64 output rows under 80 halo rows (448
+// threads, three halo rows per stage-A thread): 11-16 % faster than 48 rows in FP16.  The
+// x-half CTAs keep 48 rows (64 measured 22 % slower in FP16: the seven z sums of three rows
+// crowd the registers; in FP32 the plane boxes do not fit).
+template <int M, typename T, int XS>
+constexpr int kLpRows = XS == 1 && (sizeof(T) == 2 || M == 1) ? 64 : 48;
 
 template <int M, int N, typename T>
 inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float inv_scale,
@@ -594,7 +595,7 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
                           cudaStream_t stream, int zc0, int zc1) {
     // x-offset halves (parts 2 * split + half) or every x offset (parts = splits) per CTA
     constexpr int XS = kLpXHalf<M> ? 2 : 1;
-    using X = Lpx3d<M, N, T, kLpRows<T, XS>, XS>;
+    using X = Lpx3d<M, N, T, kLpRows<M, T, XS>, XS>;
     if (st.elem != X::ES) return cudaErrorInvalidValue;
     CUtensorMap mapR, mapC, mapD;
     const uint64_t dims[3] = {(uint64_t)st.Xs, (uint64_t)st.Yp, (uint64_t)st.Zp};
@@ -607,7 +608,7 @@ inline cudaError_t run_lp(const Staging& st, const void* staged, int tz, float i
     if (e == cudaSuccess) e = encode_tensor_map(&mapC, X::ES == 2, 3, dims, strides, boxC, base);
     if (e == cudaSuccess) e = encode_tensor_map(&mapD, X::ES == 2, 3, dims, strides, boxD, base);
     if (e != cudaSuccess) return e;
-    auto kern = nlm3d_lpx_kernel<M, N, T, kLpRows<T, XS>, XS>;
+    auto kern = nlm3d_lpx_kernel<M, N, T, kLpRows<M, T, XS>, XS>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, X::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     if (zc1 < 0) zc1 = (st.Z + tz - 1) / tz;
