@@ -101,7 +101,8 @@ int nlm_release_cached(void);
  * Compiled (sr, pr): sr 1..5 with pr 1, sr 3 and 5 with pr 2 (register-brick
  * kernel), and sr 1..6 with pr 1..8 otherwise (large-patch kernel: the
  * reference's NS 7..17 configurations), each in FP32 or FP16 storage; for the
- * latter kernel the scratch also holds two (Z, num) float pairs per voxel, or two
+ * latter kernel the scratch also holds four (Z, num) float pairs per voxel for
+ * sr >= 3 and two below (halves of the passes and of the x offsets), or as many
  * (Z, num, cZ, cnum) Kahan pairs with FP16 storage. */
 size_t nlm3d_workspace_bytes(int X, int Y, int Z, int sr, int pr, unsigned int flags);
 
