@@ -593,13 +593,16 @@ static int ensure_events(std::vector<cudaEvent_t>& v, size_t n) {
 
 // 3D host path pipelined over z chunks: the host->device copy of later input
 // chunks and the device->host copy of finished output chunks overlap the staging
-// and NLM kernels of the current chunk.  Output chunk k = planes [k CZ, (k+1) CZ),
-// CZ a multiple of the kernel's z tile; it waits only for the input planes its
-// REFLECT_101 halo reaches.  Chunks alternate between two compute streams so that
-// the kernels of chunk k+1 fill the SMs that chunk k's last wave leaves idle: chunk
-// k stages padded planes [z0 + 2H, z1 + 2H) (all of [0, z1 + 2H) for k = 0), which no
-// earlier chunk reads, and its NLM kernel waits for the staging of chunk k-1, which
-// wrote the lower 2H planes it reads.  Returns 1 when the volume is too thin to split.
+// and NLM kernels of the current chunk.  Output chunks are whole z tiles: a first and
+// a last chunk of one tile (so the first kernel waits only for the input planes its
+// REFLECT_101 halo reaches from one tile, and the last output copy is short) and
+// chunks of CZ planes between them.  Input plane k is copied in the chunk of the first
+// output chunk that reads it, so the copies run ahead of the kernels in the order they
+// are needed.  Chunks alternate between two compute streams so that the kernels of
+// chunk k+1 fill the SMs that chunk k's last wave leaves idle: chunk k stages padded
+// planes [z0 + 2H, z1 + 2H) (all of [0, z1 + 2H) for k = 0), which no earlier chunk
+// reads, and its NLM kernel waits for the staging of chunk k-1, which wrote the lower
+// 2H planes it reads.  Returns 1 when the volume is too thin to split.
 static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype, int X, int Y,
                                     int Z, int sr, int pr, float h, float* h_out,
                                     unsigned int flags) {
@@ -610,7 +613,12 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const int RZ = nlm3d_fwd_tile_z(sr, pr, fp16, variant);
     if (RZ <= 0) return 1;
     const int CZ = std::max(1, (Z / 16 + RZ - 1) / RZ) * RZ;
-    const int nch = (Z + CZ - 1) / CZ;
+    std::vector<int> zb{0};                  // output chunk boundaries
+    const int zlast = ((Z - 1) / RZ) * RZ;   // first plane of the last z tile
+    for (int z = RZ; z < zlast; z = std::min(z + CZ, zlast)) zb.push_back(z);
+    if (zlast > 0) zb.push_back(zlast);
+    zb.push_back(Z);
+    const int nch = (int)zb.size() - 1;
     if (nch < 2) return 1;
     cudaError_t e = cudaSuccess;
     if (!hp->s_h2d) e = cudaStreamCreateWithFlags(&hp->s_h2d, cudaStreamNonBlocking);
@@ -620,31 +628,33 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const Staging st = staging3d(X, Y, Z, sr, pr, fp16);
     const size_t plane_in =
         (prepadded ? (size_t)(X + 2 * H) * (Y + 2 * H) : (size_t)X * Y) * dtype_bytes(in_dtype);
-    const int in_planes = prepadded ? Z + 2 * H : Z;
-    const int nin = (in_planes + CZ - 1) / CZ;
-    int rc = ensure_events(hp->ev_in, nin);
+    int rc = ensure_events(hp->ev_in, nch);
     if (rc == NLM_OK) rc = ensure_events(hp->ev_out, nch);
     if (rc == NLM_OK) rc = ensure_events(hp->ev_st, nch);
     if (rc != NLM_OK) return rc;
+    // input planes [0, need(k)) are read by output chunks 0..k
+    auto need = [&](int k) {
+        return prepadded ? zb[k + 1] + 2 * H : std::min(Z, zb[k + 1] + H);
+    };
     const char* src = static_cast<const char*>(h_in);
     char* din = static_cast<char*>(hp->d_in);
-    for (int j = 0; j < nin; ++j) {
-        const size_t p0 = (size_t)j * CZ, p1 = std::min((size_t)in_planes, p0 + CZ);
-        e = cudaMemcpyAsync(din + p0 * plane_in, src + p0 * plane_in, (p1 - p0) * plane_in,
-                            cudaMemcpyHostToDevice, hp->s_h2d);
-        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_in[j], hp->s_h2d);
+    for (int k = 0, p0 = 0; k < nch; ++k) {
+        const int p1 = need(k);
+        if (p1 > p0)
+            e = cudaMemcpyAsync(din + (size_t)p0 * plane_in, src + (size_t)p0 * plane_in,
+                                (size_t)(p1 - p0) * plane_in, cudaMemcpyHostToDevice, hp->s_h2d);
+        if (e == cudaSuccess) e = cudaEventRecord(hp->ev_in[k], hp->s_h2d);
         if (e != cudaSuccess) return cuda_fail(e, "host->device chunk copy");
+        p0 = std::max(p0, p1);
     }
     const float s = weight_scale(pr, 3, h);
     unsigned int* ew = device_error_word();
     const size_t plane_out = (size_t)X * Y;
     for (int k = 0; k < nch; ++k) {
-        const int z0 = k * CZ, z1 = std::min(Z, z0 + CZ);
+        const int z0 = zb[k], z1 = zb[k + 1];
         const int p0 = k == 0 ? 0 : z0 + 2 * H, p1 = z1 + 2 * H;  // new padded planes
-        const int need = prepadded ? p1 - 1 : std::min(Z, z1 + H) - 1;  // last input plane read
-        const int j = std::min(nin - 1, need / CZ);
         cudaStream_t cs = (k & 1) ? hp->s_c2 : hp->stream;
-        e = cudaStreamWaitEvent(cs, hp->ev_in[j], 0);
+        e = cudaStreamWaitEvent(cs, hp->ev_in[k], 0);
         if (e == cudaSuccess) e = launch_stage(hp->d_in, in_dtype, prepadded, s, st, hp->d_ws, cs, p0, p1);
         if (e == cudaSuccess) e = cudaEventRecord(hp->ev_st[k], cs);
         if (e == cudaSuccess && k > 0) e = cudaStreamWaitEvent(cs, hp->ev_st[k - 1], 0);
