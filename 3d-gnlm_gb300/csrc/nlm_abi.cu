@@ -612,7 +612,9 @@ static int host_forward3d_pipelined(HostPath* hp, const void* h_in, int in_dtype
     const int variant = tuned_variant(3, sr, pr, fp16);
     const int RZ = nlm3d_fwd_tile_z(sr, pr, fp16, variant);
     if (RZ <= 0) return 1;
-    const int CZ = std::max(1, (Z / 16 + RZ - 1) / RZ) * RZ;
+    // about Z / 8 planes per middle chunk (256^3 end to end: 8 chunks 6794, 6: 6787,
+    // 12: 6705, 16: 6748, 24: 6688 Mvoxel/s)
+    const int CZ = std::max(1, (Z / 8 + RZ - 1) / RZ) * RZ;
     std::vector<int> zb{0};                  // output chunk boundaries
     const int zlast = ((Z - 1) / RZ) * RZ;   // first plane of the last z tile
     for (int z = RZ; z < zlast; z = std::min(z + CZ, zlast)) zb.push_back(z);
