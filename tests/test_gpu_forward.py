@@ -344,11 +344,15 @@ def test_2d_every_tile_variant(torch_cuda, gnlm_lib, fp16):
 @pytest.mark.parametrize("shape,sr,pr,fp16,u8_prepadded", [
     ((37, 30, 50), 3, 1, False, False), ((64, 20, 33), 5, 1, False, False),
     ((41, 28, 40), 3, 1, True, False), ((33, 24, 31), 3, 2, False, False),
-    ((48, 36, 40), 3, 1, False, True)])
+    ((48, 36, 40), 3, 1, False, True), ((7, 20, 30), 3, 1, False, False),
+    ((13, 20, 30), 3, 1, False, False), ((130, 17, 23), 2, 1, False, False),
+    ((70, 40, 36), 4, 5, False, False)])
 def test_3d_pipelined_host_path_matches_device_path(torch_cuda, gnlm_lib, shape, sr, pr, fp16,
                                                     u8_prepadded):
-    """The host-buffer call overlaps its copies with compute over z chunks; the
-    result must equal the device-buffer call exactly."""
+    """The host-buffer call overlaps its copies with compute over z chunks (a first and
+    a last chunk of one z tile, larger ones between; 7 and 13 planes give two and three
+    chunks, 130 planes many, the large-patch case chunks by its chunk depth); the result
+    must equal the device-buffer call exactly."""
     torch = torch_cuda
     v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=6, sigma=0.05, seed=sum(shape) + sr)
     h = 0.05
