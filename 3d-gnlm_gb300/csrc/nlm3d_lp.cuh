@@ -7,11 +7,11 @@
 // with the patch; here every box sum is a running sum and the cost per (voxel,
 // offset) does not depend on the patch width.
 //
-// A CTA owns a column tile of 32 x 48 output voxels, a chunk of TZ planes and, from
-// search radius 3, one half of the x offsets (ox = -M..0 or 1..M; below that every x
-// offset).  It makes (2sr+1)^2 passes, one per (oz, oy); a pass streams the chunk's
+// A CTA owns a column tile of 32 x 48 output voxels (32 x 64 where the buffers fit), a
+// chunk of TZ planes and, from search radius 3, one half of the x offsets (ox = -M..0
+// or 1..M; below that every x offset).  It makes (2sr+1)^2 passes, one per (oz, oy); a pass streams the chunk's
 // planes (plus the patch halo) in z, each step in four barrier-separated stages:
-//   A  each thread owns 4 halo columns of two halo rows and keeps, per x offset, the
+//   A  each thread owns 4 halo columns of two (or three) halo rows and keeps, per x offset, the
 //      running z-sum Sz of squared differences over the 2pr+1 planes around the
 //      current plane (add the entering plane, subtract the leaving one; the first
 //      window is built two planes per step); the reference and candidate planes of
@@ -32,9 +32,9 @@
 // the TMA plane boxes hold FP16, halving their bytes; every difference, square and
 // sum is FP32, and the per-pass weight sums are added across passes with Kahan
 // compensation, the (Z, num) accumulator then holding (Z, num, cZ, cnum)).  TMA needs
-// 16-byte aligned box starts and widths, so for FP16 the boxes start 8 elements
-// before the tile (candidate box) or on the 8-element boundary below the first
-// halo group (reference box) and the in-box column offsets CB and RO absorb that.
+// 16-byte aligned box starts and widths, so for FP16 each box starts on the 8-element
+// boundary at or below its first 4-column group and the in-box column offsets (CB, RO,
+// CB0, CB1) absorb that.
 #pragma once
 
 #include <algorithm>
