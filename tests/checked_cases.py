@@ -42,13 +42,26 @@ def run_cases(gnlm, torch):
     for sr, pr in [(6, 8), (1, 3)]:
         res[f"lp16_{sr}_{pr}"] = gnlm.nlm3d_forward(xl, sr, pr, 0.05,
                                                     fp16_storage=True).cpu().numpy()
+    # every compiled 3D pair in both storage forms, on a shape with a second tile on every
+    # tiled axis of every kernel (50 rows: two 48-row large-patch tiles, one 64-row tile)
+    vp, _ = phantom.ellipsoid_phantom((9, 50, 37), n_ellipsoids=4, sigma=0.05, seed=77,
+                                      radii=(1.5, 8.0))
+    xp = torch.from_numpy(vp).cuda()
+    for sr in range(1, 7):
+        for pr in range(1, 9):
+            for fp16 in (False, True):
+                res[f"pair_{sr}_{pr}_f{int(fp16)}"] = gnlm.nlm3d_forward(
+                    xp, sr, pr, 0.05, fp16_storage=fp16).cpu().numpy()
     im, _ = phantom.disc_rect_phantom((61, 90), n_shapes=6, sigma=0.08, seed=5)
     x2 = torch.from_numpy(im).cuda()
     for var in range(gnlm.variant_count(2, False)):
         gnlm.set_variant(2, 5, 2, var)
         res[f"2d_s5p2_v{var}"] = gnlm.nlm2d_forward(x2, 5, 2, 0.08).cpu().numpy()
     gnlm.set_variant(2, 5, 2, -1)
-    res["2d_s10p5"] = gnlm.nlm2d_forward(x2, 10, 5, 0.08).cpu().numpy()
+    for sr, pr in [(1, 1), (3, 1), (5, 1), (3, 2), (7, 2), (3, 5), (7, 5), (10, 5)]:
+        for fp16 in (False, True):
+            res[f"2d_s{sr}p{pr}_f{int(fp16)}"] = gnlm.nlm2d_forward(
+                x2, sr, pr, 0.08, fp16_storage=fp16).cpu().numpy()
     va, _ = phantom.ellipsoid_phantom((10, 12, 40), n_ellipsoids=3, sigma=0.05, seed=6,
                                       radii=(1.5, 5.0))
     xa = torch.from_numpy(va).cuda()
