@@ -17,7 +17,8 @@
 // Kernels: adj_aux_kernel ((G, out') pairs padded like the staged volume),
 // nlm3d_adj_kernel (gpad' over the padded domain + per-CTA h partial sums; the
 // tiles of a last, partial wave are split by offset runs over several CTAs whose
-// partial gpad' adj_tail_combine_kernel adds in part order),
+// partial gpad' adj_tail_combine_kernel adds in part order; with patch radius 1 the z
+// offsets go in groups that stream each candidate and (G, out') plane once, adj_zgroup),
 // adj_fold_kernel (REFLECT_101 fold, times s), adj_hgrad_kernel (fixed-order sum).
 #include <cuda_fp16.h>
 
@@ -112,6 +113,134 @@ __device__ __forceinline__ float2 xbox_pair(float2 y) {
     }
 }
 
+// Offset runs of one tile: (oz, oy) pairs, or (z group, oy) pairs when the z offsets are
+// grouped by GZ.
+template <int M, int GZ>
+__host__ __device__ constexpr int adj_runs() {
+    return GZ > 0 ? (2 * M + 1 + GZ - 1) / GZ * (2 * M + 1) : (2 * M + 1) * (2 * M + 1);
+}
+
+// The offsets (ox, oy, oz + g), g < G, of one z group, ox = -M..M, for patch radius 1.
+// The thread streams the group's candidate planes c = 0 .. PT + G - 2 of its difference
+// window once: plane c is difference plane c - g of offset oz + g, so one candidate load
+// serves G offsets, and the (G, out') plane c - 2 serves distance plane c - 2 - g of each.
+// Per offset the stream keeps three-plane rings of squared differences (z box of t^2),
+// of t at the output rows (the t A term) and of the field a (z box of a); distance plane
+// pd completes at difference plane pd + 2 and output plane q at distance plane q + 2.
+// Within each offset the arithmetic is the window form's (the same sums in the same
+// order: plane pairs share the middle terms of their z boxes, row pairs of their y boxes).
+template <int M, int RY, int RZ, int NW, int G>
+__device__ __forceinline__ void adj_zgroup(const float* vt, const float2* got, int sx, int sy,
+                                           int sz, int oz, int oy,
+                                           const float2 (&av)[(RY + 4) / 2][RZ + 4],
+                                           const float2 (&gref)[RY + 2][RZ + 2],
+                                           float (&acc_e)[RY][RZ], float (&acc_t)[RY][RZ],
+                                           float& hrun) {
+    constexpr int N = 1;
+    using C = Adj3d<M, N, RY, RZ, NW>;
+    constexpr int RT = C::RT, PT = C::PT, RD = C::RD, RTP = RT / 2;
+    constexpr int CEND = PT + G - 1;
+    const float2 minus1 = make_float2(-1.f, -1.f);
+    auto avs = [&](int r, int p) { return (r & 1) ? av[r >> 1][p].y : av[r >> 1][p].x; };
+    for (int ox = -M; ox <= M; ++ox) {
+        const int off = oz * C::PLANE + oy * C::BX + ox;
+        const float* cb = vt + (sz - 2 * N) * C::PLANE + (sy - 2 * N) * C::BX + sx + off;
+        const float2* gb = got + (sz - N) * C::PLANE + (sy - N) * C::BX + sx + off;
+        float2 sq[G][3][RTP];  // t^2 of difference planes jj % 3, row pairs
+        float2 zmid[G][RTP];   // sq(pd + 1) + sq(pd + 2) of an even distance plane pd
+        float2 tt[G][3][RY / 2];  // t at rows 2 .. RY + 1 of difference planes jj % 3
+        float ar[G][3][RD];    // a of distance planes pd % 3
+        float amid[G][RD];     // a(q + 1) + a(q + 2) of an even output plane q
+        float bprev[RT];       // the previous candidate plane (v'_{w+o} of distance plane pd)
+#pragma unroll
+        for (int c = 0; c < CEND; ++c) {
+            float bc[RT];
+#pragma unroll
+            for (int r = 0; r < RT; ++r) bc[r] = cb[c * C::PLANE + r * C::BX];
+            float2 gpl[RD];  // (G, out') at plane c - 2 of the distance window (offset oz)
+            if (c >= 2 * N) {
+#pragma unroll
+                for (int r = 0; r < RD; ++r) gpl[r] = gb[(c - 2 * N) * C::PLANE + r * C::BX];
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int jj = c - g;  // difference plane of offset oz + g
+                if (jj < 0 || jj >= PT) continue;
+                float2 s2[RTP];
+#pragma unroll
+                for (int rp = 0; rp < RTP; ++rp) {
+                    const float2 t = __ffma2_rn(make_float2(bc[2 * rp], bc[2 * rp + 1]), minus1,
+                                                av[rp][jj]);
+                    s2[rp] = __fmul2_rn(t, t);
+                    if (rp >= 1 && rp <= RY / 2) tt[g][jj % 3][rp - 1] = t;
+                }
+                if (jj >= 2 * N) {
+                    const int pd = jj - 2 * N;  // distance plane completed by this plane
+                    float zrow[RT];
+#pragma unroll
+                    for (int rp = 0; rp < RTP; ++rp) {
+                        float2 z;
+                        if ((pd & 1) == 0) {
+                            zmid[g][rp] = __fadd2_rn(sq[g][(jj - 1) % 3][rp], s2[rp]);
+                            z = __fadd2_rn(sq[g][(jj - 2) % 3][rp], zmid[g][rp]);
+                        } else {
+                            z = __fadd2_rn(zmid[g][rp], s2[rp]);
+                        }
+                        zrow[2 * rp] = z.x;
+                        zrow[2 * rp + 1] = z.y;
+                    }
+                    float D[RD];
+                    box_pairs<3, RD>(zrow, D);
+#pragma unroll
+                    for (int r = 0; r < RD; r += 2) {
+                        const float2 x2 = xbox_pair<N>(make_float2(D[r], D[r + 1]));
+                        D[r] = x2.x;
+                        D[r + 1] = x2.y;
+                    }
+#pragma unroll
+                    for (int r = 0; r < RD; ++r) {
+                        const float2 go2 = gpl[r];
+                        const float e = ex2_neg(D[r]);
+                        const float gd = gref[r][pd].x * (bprev[r + N] - gref[r][pd].y);
+                        ar[g][pd % 3][r] = e * fmaf(go2.x, avs(r + N, pd + N) - go2.y, gd);
+                        const int q = pd - N;
+                        if (r >= N && r < N + RY && q >= 0 && q < RZ) {
+                            acc_e[r - N][q] = fmaf(go2.x, e, acc_e[r - N][q]);
+                            hrun = fmaf(e * gd, D[r], hrun);
+                        }
+                    }
+                    if (pd >= 2 * N) {
+                        const int q = pd - 2 * N;  // output plane completed
+                        float za[RD];
+#pragma unroll
+                        for (int r = 0; r < RD; ++r) {
+                            if ((q & 1) == 0) {
+                                amid[g][r] = ar[g][(pd - 1) % 3][r] + ar[g][pd % 3][r];
+                                za[r] = ar[g][(pd - 2) % 3][r] + amid[g][r];
+                            } else {
+                                za[r] = amid[g][r] + ar[g][pd % 3][r];
+                            }
+                        }
+                        float Ay[RY];
+                        box_pairs<3, RY>(za, Ay);
+#pragma unroll
+                        for (int r = 0; r < RY; r += 2) {
+                            const float2 A = xbox_pair<N>(make_float2(Ay[r], Ay[r + 1]));
+                            const float2 t = tt[g][pd % 3][r / 2];  // t at rows r + 2, r + 3
+                            acc_t[r][q] = fmaf(t.x, A.x, acc_t[r][q]);
+                            acc_t[r + 1][q] = fmaf(t.y, A.y, acc_t[r + 1][q]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int rp = 0; rp < RTP; ++rp) sq[g][jj % 3][rp] = s2[rp];
+            }
+#pragma unroll
+            for (int r = 0; r < RT; ++r) bprev[r] = bc[r];
+        }
+    }
+}
+
 // Work split of one launch (1D grid): CTAs [0, full) own tiles [0, full) whole;
 // each of the ntail tiles after them is split into S parts, CTA full + t*S + p
 // making part p of the (2M+1)^2 (oz, oy) offset runs of tile full + t and writing
@@ -124,7 +253,9 @@ struct AdjTail {
     float* side;  // S * ntail partial bricks (tile_vox floats each)
 };
 
-template <int M, int N, int RY, int RZ, int NW>
+// GZ = 0: one offset at a time over the whole window.  GZ > 0 (patch radius 1): the z
+// offsets in groups of GZ, streamed plane by plane (adj_zgroup below).
+template <int M, int N, int RY, int RZ, int NW, int GZ>
 __global__ void __launch_bounds__(32 * NW, 1)
     nlm3d_adj_kernel(const __grid_constant__ CUtensorMap vmap,
                      const __grid_constant__ CUtensorMap gomap, int X, int Y, int Z, int Xs, int Yp,
@@ -141,8 +272,9 @@ __global__ void __launch_bounds__(32 * NW, 1)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int Xp = X + 2 * C::H, Ypd = Y + 2 * C::H, Zp = Z + 2 * C::H;
-    // Tile and offset runs of this CTA (uniform over the CTA).
-    constexpr int RUNS = (2 * M + 1) * (2 * M + 1);
+    // Tile and offset runs of this CTA (uniform over the CTA): (oz, oy) pairs, or (z group,
+    // oy) pairs with grouped z offsets.
+    constexpr int RUNS = adj_runs<M, GZ>();
     int tile, part = 0, nparts = 1;
     if ((int)blockIdx.x < tl.full) {
         tile = blockIdx.x;
@@ -221,6 +353,19 @@ __global__ void __launch_bounds__(32 * NW, 1)
     double hacc = 0.0;
     const float2 minus1 = make_float2(-1.f, -1.f);
 
+    if constexpr (GZ > 0) {
+        constexpr int ZG = (2 * M + 1 + GZ - 1) / GZ, GR = (2 * M + 1) - (ZG - 1) * GZ;
+        for (int run = run0; run < run1; ++run) {
+            const int gi = run / (2 * M + 1), oy = run % (2 * M + 1) - M;
+            const int oz = -M + gi * GZ;
+            float hrun = 0.f;
+            if (gi < ZG - 1)
+                adj_zgroup<M, RY, RZ, NW, GZ>(vt, got, sx, sy, sz, oz, oy, av, gref, acc_e, acc_t, hrun);
+            else
+                adj_zgroup<M, RY, RZ, NW, GR>(vt, got, sx, sy, sz, oz, oy, av, gref, acc_e, acc_t, hrun);
+            hacc += (double)hrun;
+        }
+    } else
     for (int run = run0; run < run1; ++run) {
         const int oz = run / (2 * M + 1) - M, oy = run % (2 * M + 1) - M;
         {
@@ -499,7 +644,7 @@ static AdjTail adj_tail_plan(int nx, int ny, int nz, int runs) {
     return t;
 }
 
-template <int M, int N, int RY, int RZ, int NW>
+template <int M, int N, int RY, int RZ, int NW, int GZ>
 static cudaError_t run_adj3d(const Staging& st, const void* staged, const float* d_out,
                              const float* d_zsum, const float* d_gout, float s, float h,
                              float* gin, double* hgrad, float2* GO, float* gpad,
@@ -522,11 +667,11 @@ static cudaError_t run_adj3d(const Staging& st, const void* staged, const float*
     if ((e = encode_tensor_map(&vmap, false, 3, dims, strides, box, const_cast<void*>(staged))))
         return e;
     if ((e = encode_tensor_map(&gomap, false, 3, dims2, strides2, box2, GO))) return e;
-    auto kern = nlm3d_adj_kernel<M, N, RY, RZ, NW>;
+    auto kern = nlm3d_adj_kernel<M, N, RY, RZ, NW, GZ>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES)))
         return e;
     AdjTail tl = adj_tail_plan((st.Xp + C::XO - 1) / C::XO, (st.Yp + C::TY - 1) / C::TY,
-                               (st.Zp + RZ - 1) / RZ, (2 * M + 1) * (2 * M + 1));
+                               (st.Zp + RZ - 1) / RZ, adj_runs<M, GZ>());
     tl.side = side;
     const int nblk = tl.full + tl.S * tl.ntail;
     kern<<<nblk, 32 * NW, C::SMEM_BYTES, stream>>>(vmap, gomap, st.X, st.Y, st.Z, st.Xs, st.Yp,
@@ -549,12 +694,19 @@ static cudaError_t run_adj3d(const Staging& st, const void* staged, const float*
     return e;
 }
 
+// Z offsets per group of the patch-radius-1 adjoint: at most GMAX, the 2M + 1 offsets
+// split into equal groups where they divide (9 -> 5 + 4, 11 -> 6 + 5, 7 -> 2+2+2+1).
+constexpr int adj_group(int n, int gmax) { return (n + (n + gmax - 1) / gmax - 1) / ((n + gmax - 1) / gmax); }
+
 // Tile shape per (sr, pr): 8 warps x 2 rows x 4 planes, or 4 x 2 x 2 where the
 // three FP32 tiles of a larger halo would not fit in shared memory.
 template <int M, int N>
 struct AdjShape {
     static constexpr bool SMALL = M + 2 * N > 5;
     static constexpr int RY = 2, RZ = SMALL ? 2 : 4, NW = SMALL ? 4 : 8;
+    // z offsets per group (patch 3): the 2-plane tiles hold six offsets' rings within the
+    // register budget (232-254 registers), the 4-plane tiles two (252 registers)
+    static constexpr int GZ = N == 1 ? adj_group(2 * M + 1, SMALL ? 6 : 2) : 0;
     using C = Adj3d<M, N, RY, RZ, NW>;
 };
 
@@ -600,7 +752,8 @@ cudaError_t launch_nlm3d_adj(const Staging& st, const void* staged, const float*
     if (st.H > kMaxHalo) return cudaErrorNotSupported;
 #define X_(m, n)                                                                                \
     if (sr == m && pr == n)                                                                     \
-        return run_adj3d<m, n, AdjShape<m, n>::RY, AdjShape<m, n>::RZ, AdjShape<m, n>::NW>(    \
+        return run_adj3d<m, n, AdjShape<m, n>::RY, AdjShape<m, n>::RZ, AdjShape<m, n>::NW,     \
+                         AdjShape<m, n>::GZ>(                                                   \
             st, staged, d_out, d_zsum, d_gout, s, h, gin, hgrad, GO, gpad, hpart, side,         \
             errword, stream);
     GNLM_ADJ3D_CASES(X_)

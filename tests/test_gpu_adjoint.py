@@ -30,11 +30,15 @@ def _run(torch, gnlm, v, sr, pr, h, g):
 
 # One CTA per SM: grids under a wave split every tile into offset-run parts; on a
 # 152-SM GB300, (40, 60, 56) is 180 tiles = 152 whole + 28 tail tiles in 5 parts each,
-# and (50, 40, 48) is 90 tiles, too many for a split (each tile made whole).
+# and (50, 40, 48) is 90 tiles, too many for a split (each tile made whole).  Search 9 and
+# 11 run 2-plane tiles with z offsets in groups of 5 + 4 and 6 + 5: (24, 30, 28) is 170
+# tiles (18 tail tiles in 8 parts), (20, 30, 26) 192 (40 in 3 parts).
 @pytest.mark.parametrize("shape,sr,pr", [((8, 10, 12), 2, 1), ((12, 13, 14), 3, 1),
                                          ((9, 11, 40), 1, 1), ((10, 12, 12), 3, 2),
                                          ((7, 9, 11), 5, 1), ((3, 4, 5), 3, 1),
-                                         ((40, 60, 56), 3, 1), ((50, 40, 48), 3, 1)])
+                                         ((40, 60, 56), 3, 1), ((50, 40, 48), 3, 1),
+                                         ((11, 14, 13), 4, 1), ((24, 30, 28), 4, 1),
+                                         ((20, 30, 26), 5, 1)])
 def test_adjoint_matches_fp64_oracle(torch_cuda, gnlm_lib, shape, sr, pr):
     v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=4, sigma=0.05, seed=sum(shape) + sr,
                                      radii=(1.5, 6.0))
