@@ -66,7 +66,7 @@ def run_cases(gnlm, torch):
                                       radii=(1.5, 5.0))
     xa = torch.from_numpy(va).cuda()
     g = torch.from_numpy(np.random.default_rng(7).standard_normal(va.shape).astype(np.float32)).cuda()
-    for sr, pr in [(3, 1), (3, 2)]:
+    for sr, pr in [(3, 1), (3, 2), (1, 1), (4, 1), (5, 1)]:
         out, zs = gnlm.nlm3d_forward(xa, sr, pr, 0.06, return_zsum=True)
         gin, hg = gnlm.nlm3d_adjoint(xa, out, zs, g, sr, pr, 0.06)
         res[f"adj_{sr}_{pr}"] = gin.cpu().numpy()
