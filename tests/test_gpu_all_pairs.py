@@ -16,10 +16,11 @@ _ORACLE = {}
 
 
 def _oracle(fn, a, sr, pr, h):
-    """FP64 oracle output, computed once per (input, pair) for both storage forms."""
+    """FP64 oracle (output, weight sum Z), computed once per (input, pair) for both storage
+    forms."""
     key = (fn.__name__, a.shape, sr, pr)
     if key not in _ORACLE:
-        _ORACLE[key] = fn(a, sr, pr, h, dtype=np.float64)
+        _ORACLE[key] = fn(a, sr, pr, h, dtype=np.float64, return_z=True)
     return _ORACLE[key]
 
 BRICK3D = [(1, 1), (2, 1), (3, 1), (4, 1), (5, 1), (3, 2), (5, 2)]
@@ -36,37 +37,46 @@ def test_pair_lists_cover_every_search_patch_combination():
     assert both == {(sr, pr) for sr in range(1, 7) for pr in range(1, 9)}
 
 
+# (9, 50, 37): a second tile on every tiled axis; (2, 3, 5) and (1, 1, 1): every extent
+# below the halo, so REFLECT_101 folds each axis repeatedly (a single voxel reflects onto
+# itself, out = in).
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(9, 50, 37), (2, 3, 5), (1, 1, 1)])
 @pytest.mark.parametrize("fp16", [False, True], ids=["f32", "f16"])
-def test_3d_every_compiled_pair(torch_cuda, gnlm_lib, fp16):
+def test_3d_every_compiled_pair(torch_cuda, gnlm_lib, fp16, shape):
     torch = torch_cuda
-    v, _ = phantom.ellipsoid_phantom((9, 50, 37), n_ellipsoids=4, sigma=0.05, seed=77,
+    v, _ = phantom.ellipsoid_phantom(shape, n_ellipsoids=4, sigma=0.05, seed=77,
                                      radii=(1.5, 8.0))
     x = torch.from_numpy(v).cuda()
     tol = TOL_F16 if fp16 else TOL_F32
     worst = {}
     for sr, pr in BRICK3D + LP3D:
-        o = _oracle(O.nlm3d, v, sr, pr, 0.05)
-        g = gnlm_lib.nlm3d_forward(x, sr, pr, 0.05, fp16_storage=fp16).cpu().numpy()
-        worst[(sr, pr)] = float(np.abs(g - o).max())
-    bad = {k: e for k, e in worst.items() if not e <= tol}
+        o, oz = _oracle(O.nlm3d, v, sr, pr, 0.05)
+        g, gz = gnlm_lib.nlm3d_forward(x, sr, pr, 0.05, fp16_storage=fp16, return_zsum=True)
+        err = float(np.abs(g.cpu().numpy() - o).max())
+        zerr = 0.0 if fp16 else float(np.abs(gz.cpu().numpy() / oz - 1).max())
+        worst[(sr, pr)] = (err, zerr)
+    bad = {k: e for k, e in worst.items() if not (e[0] <= tol and e[1] <= 1e-5)}
     assert not bad, bad
     assert gnlm_lib.device_status() == (0, 0)
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(45, 131), (3, 5), (1, 1)])
 @pytest.mark.parametrize("fp16", [False, True], ids=["f32", "f16"])
-def test_2d_every_compiled_pair(torch_cuda, gnlm_lib, fp16):
+def test_2d_every_compiled_pair(torch_cuda, gnlm_lib, fp16, shape):
     torch = torch_cuda
-    im, _ = phantom.disc_rect_phantom((45, 131), n_shapes=6, sigma=0.08, seed=78)
+    im, _ = phantom.disc_rect_phantom(shape, n_shapes=6, sigma=0.08, seed=78)
     x = torch.from_numpy(im).cuda()
     tol = TOL_F16 if fp16 else TOL_F32
     worst = {}
     for sr, pr in FWD2D:
-        o = _oracle(O.nlm2d, im, sr, pr, 0.08)
-        g = gnlm_lib.nlm2d_forward(x, sr, pr, 0.08, fp16_storage=fp16).cpu().numpy()
-        worst[(sr, pr)] = float(np.abs(g - o).max())
-    bad = {k: e for k, e in worst.items() if not e <= tol}
+        o, oz = _oracle(O.nlm2d, im, sr, pr, 0.08)
+        g, gz = gnlm_lib.nlm2d_forward(x, sr, pr, 0.08, fp16_storage=fp16, return_zsum=True)
+        err = float(np.abs(g.cpu().numpy() - o).max())
+        zerr = 0.0 if fp16 else float(np.abs(gz.cpu().numpy() / oz - 1).max())
+        worst[(sr, pr)] = (err, zerr)
+    bad = {k: e for k, e in worst.items() if not (e[0] <= tol and e[1] <= 1e-5)}
     assert not bad, bad
     assert gnlm_lib.device_status() == (0, 0)
 
