@@ -696,7 +696,10 @@ static cudaError_t run_adj3d(const Staging& st, const void* staged, const float*
 
 // Z offsets per group of the patch-radius-1 adjoint: at most GMAX, the 2M + 1 offsets
 // split into equal groups where they divide (9 -> 5 + 4, 11 -> 6 + 5, 7 -> 2+2+2+1).
-constexpr int adj_group(int n, int gmax) { return (n + (n + gmax - 1) / gmax - 1) / ((n + gmax - 1) / gmax); }
+constexpr int adj_group(int n, int gmax) {
+    const int groups = (n + gmax - 1) / gmax;
+    return (n + groups - 1) / groups;
+}
 
 // Tile shape per (sr, pr): 8 warps x 2 rows x 4 planes, or 4 x 2 x 2 where the
 // three FP32 tiles of a larger halo would not fit in shared memory.
